@@ -1,0 +1,53 @@
+"""Build recipe for the oracle (test infrastructure only).
+
+* oracle/_build/liboracle.so  -- the C++ restatement (oracle.cpp), always.
+* oracle/_ref/libref_pin.so   -- the reference's own _yooji_math_inlines.h
+  compiled from the reference tree, only where that tree is present.
+
+No -march flags: the same source must build on x86-64 and aarch64.
+-ffp-contract=off keeps GCC from fusing multiply-adds (the CUDA side builds
+with -fmad=false), so both sides round every operation the same way.
+"""
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_UTIL = "/root/reference/VCL_Volume_Scanner/STAC/Util"
+CXX = os.environ.get("CXX", "g++")
+FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
+
+
+def _newer(out, srcs):
+    if not os.path.exists(out):
+        return False
+    t = os.path.getmtime(out)
+    return all(os.path.getmtime(s) <= t for s in srcs)
+
+
+def build_oracle(force=False):
+    out = os.path.join(HERE, "_build", "liboracle.so")
+    srcs = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle.h")]
+    if force or not _newer(out, srcs):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        subprocess.check_call([CXX] + FLAGS + ["-o", out, srcs[0]])
+    return out
+
+
+def build_ref_pin(force=False):
+    """Returns the path of libref_pin.so, or None when the reference tree is absent."""
+    if not os.path.isdir(REF_UTIL):
+        return None
+    out = os.path.join(HERE, "_ref", "libref_pin.so")
+    src = os.path.join(HERE, "ref_pin.cpp")
+    hdr = os.path.join(REF_UTIL, "_yooji_math_inlines.h")
+    if force or not _newer(out, [src, hdr]):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        subprocess.check_call([CXX] + FLAGS + ["-fpermissive", "-w", "-I", REF_UTIL, "-o", out, src])
+    return out
+
+
+if __name__ == "__main__":
+    force = "--force" in sys.argv
+    print(build_oracle(force))
+    print(build_ref_pin(force))

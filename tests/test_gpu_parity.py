@@ -1,0 +1,307 @@
+"""Parity of the CUDA path (through the C ABI) with the CPU oracle.
+
+Tolerances (the project's contract): filtered depth within 1e-5 m; per-frame
+ICP pose within 1e-4 rad and 0.1 mm; TSDF within one int16 step and weights
+bit-exact; ray-cast vertices within 1 mm on 99.9 % of valid pixels.  Stages
+are compared on identical inputs, so most comparisons are in fact exact."""
+import ctypes
+
+import numpy as np
+import pytest
+
+import helpers
+import oracle_py as O
+import vs_scanner as V
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+
+def dev(a):
+    """host numpy -> CUDA tensor (kept alive by the caller)"""
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def run_filter(sess, depth_mm):
+    t = dev(depth_mm.astype(np.uint16).view(np.int16))
+    sess.stage_filter(t.data_ptr())
+    sess.sync()
+    return t
+
+
+@pytest.fixture(scope="module")
+def case(gpu):
+    return helpers.make_case(width=160, height=120, dim=128, frames=5, seed=3, dropout_blob=0.01)
+
+
+# ---------------------------------------------------------------------------
+# a1, a2, a4: ingest, bilateral, pyramid
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("kind", ["synthetic", "constant", "holes", "zero", "max"])
+def test_filter_and_pyramid(gpu, case, kind):
+    cfg = case["cfg"]
+    h, w = cfg.height, cfg.width
+    if kind == "synthetic":
+        mm = case["depth"][0]
+    elif kind == "constant":
+        mm = np.full((h, w), 1234, np.uint16)
+    elif kind == "holes":
+        mm = case["depth"][1].copy()
+        mm[10:30, 20:60] = 0
+        mm[::7, ::5] = 0
+    elif kind == "zero":
+        mm = np.zeros((h, w), np.uint16)
+    else:
+        mm = np.full((h, w), 65535, np.uint16)
+    with V.Session(cfg) as s:
+        run_filter(s, mm)
+        raw_host = s.input_raw()
+        ref_raw = O.depth_to_m(mm)
+        assert np.array_equal(raw_host, ref_raw)
+        ref = [O.bilateral(ref_raw)]
+        for l in range(1, 3):
+            ref.append(O.pyramid_down(ref[-1]))
+        got = [s.maps(l)["input_depth"] for l in range(3)]
+        for l in range(3):
+            assert np.max(np.abs(got[l] - ref[l])) <= 1e-5, (kind, l)
+            # zeros (holes) must coincide exactly
+            assert np.array_equal(got[l] == 0, ref[l] == 0), (kind, l)
+        # the pyramid kernel is exact given the same level-0 input
+        for l in range(1, 3):
+            assert np.array_equal(got[l], O.pyramid_down(got[l - 1]))
+
+
+def test_bilateral_reference_entry_points(gpu, case):
+    cfg = case["cfg"]
+    d = O.depth_to_m(case["depth"][2])
+    with V.Session(cfg) as s:
+        out = s.bfd_bilateral_filter_depth_host(d)
+        assert np.max(np.abs(out - O.bilateral(d))) <= 1e-5
+        o = torch.zeros(d.size, dtype=torch.float32, device="cuda")
+        s.bfd_bilateral_filter_depth(o.data_ptr(), d)
+        assert np.array_equal(o.cpu().numpy().reshape(d.shape), out)
+
+
+# ---------------------------------------------------------------------------
+# a5: input vertex / normal maps (with the in-place rejection recurrence)
+# ---------------------------------------------------------------------------
+def test_input_vertex_normal_maps(gpu):
+    c = helpers.make_case(width=320, height=240, dim=128, frames=1, seed=9, cos_normal=np.cos(np.radians(20)))
+    cfg = c["cfg"]
+    K = O.level_K(c["ocfg"])
+    with V.Session(cfg) as s:
+        run_filter(s, c["depth"][0])
+        for l in range(3):
+            m = s.maps(l)
+            v, n = O.point_normal_map(m["input_depth"], K[l])
+            assert np.array_equal(m["input_vertex"], v), l
+            assert np.array_equal(m["input_normal"], n), l
+            # the recurrence matters on this scene: some normals are rejected
+            if l == 0:
+                assert (v[..., 0] == -100).sum() > (m["input_depth"] <= 0).sum()
+
+
+# ---------------------------------------------------------------------------
+# a9, a10: sub-cube activation and TSDF update
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("tsdf_type", [V.VS_TSDF_INT16, V.VS_TSDF_FP16, V.VS_TSDF_FP32])
+def test_integrate_identical_inputs(gpu, case, tsdf_type):
+    cfg = helpers.make_case(width=160, height=120, dim=128, frames=1, seed=3, tsdf_type=tsdf_type)["cfg"]
+    ocfg = O.config_from_vs(cfg)
+    vol = O.Volume(ocfg)
+    with V.Session(cfg) as s:
+        for k in range(4):
+            raw = O.depth_to_m(case["depth"][k])
+            Tgc = case["gt"][k].astype(np.float32)
+            Tcg = O.pose_inverse(Tgc)
+            vol.integrate(raw, Tgc, Tcg)
+            d_raw, d_gc, d_cg = dev(raw), dev(Tgc), dev(Tcg)
+            s.cdtoc_convert_depth_to_tsdf(d_raw.data_ptr(), d_gc.data_ptr(), d_cg.data_ptr())
+            # same set of activated sub-cubes
+            act = np.sort(s.active_bricks())
+            assert np.array_equal(act, np.nonzero(vol.flags())[0].astype(np.uint32)), k
+        t, wgt = s.volume()
+    ot, ow = vol.get()
+    assert np.array_equal(wgt, ow)
+    m = ow > 0
+    if tsdf_type == V.VS_TSDF_INT16:
+        assert np.max(np.abs(helpers.q16(t[m]) - helpers.q16(ot[m]))) <= 1
+    else:
+        assert np.array_equal(t[m], ot[m])
+    assert m.sum() > 10000
+
+
+def test_integrate_max_weight_freezes(gpu):
+    c = helpers.make_case(width=80, height=60, dim=64, frames=1, seed=4)
+    cfg = c["cfg"]
+    cfg.max_w = 3.0
+    ocfg = O.config_from_vs(cfg)
+    vol = O.Volume(ocfg)
+    raw = O.depth_to_m(c["depth"][0])
+    I = np.eye(4, dtype=np.float32)
+    with V.Session(cfg) as s:
+        d_raw, d_i = dev(raw), dev(I)
+        for _ in range(5):
+            vol.integrate(raw, I, I)
+            s.cdtoc_convert_depth_to_tsdf(d_raw.data_ptr(), d_i.data_ptr(), d_i.data_ptr())
+        t, w = s.volume()
+    ot, ow = vol.get()
+    assert w.max() == 3 and np.array_equal(w, ow)
+    assert np.array_equal(helpers.q16(t[ow > 0]), helpers.q16(ot[ow > 0]))
+
+
+# ---------------------------------------------------------------------------
+# a11, a12: ray casting on an identical volume
+# ---------------------------------------------------------------------------
+def test_raycast_identical_volume(gpu, case):
+    cfg, ocfg = case["cfg"], case["ocfg"]
+    vol = O.Volume(ocfg)
+    for k in range(3):
+        raw = O.depth_to_m(case["depth"][k])
+        Tgc = case["gt"][k].astype(np.float32)
+        vol.integrate(raw, Tgc, O.pose_inverse(Tgc))
+    t, w = vol.get()
+    Tgc = case["gt"][3].astype(np.float32)
+    Tcg = O.pose_inverse(Tgc)
+    cam = O.camera_center(Tgc)
+    light = np.array([0, 0, -1], np.float32)
+    with V.Session(cfg) as s:
+        s.set_volume(t, w)
+        gt2, gw2 = s.volume()
+        assert np.array_equal(gw2, w)
+        d_gc, d_cg = dev(Tgc), dev(Tcg)
+        for l, (lw, lh, *_k) in enumerate(s.levels):
+            od, ov, on, oi = vol.raycast(l, Tgc, Tcg, cam, light)
+            gd = torch.zeros(lw * lh, dtype=torch.float32, device="cuda")
+            gv = torch.zeros(3 * lw * lh, dtype=torch.float32, device="cuda")
+            gn = torch.zeros(3 * lw * lh, dtype=torch.float32, device="cuda")
+            gi = torch.zeros(lw * lh, dtype=torch.uint8, device="cuda")
+            s.rmi_render_maps_for_icp(l, d_gc.data_ptr(), d_cg.data_ptr(), cam, light, gd.data_ptr(),
+                                      gv.data_ptr(), gn.data_ptr(), gi.data_ptr())
+            gd = gd.cpu().numpy().reshape(lh, lw)
+            gv = gv.cpu().numpy().reshape(lh, lw, 3)
+            gn = gn.cpu().numpy().reshape(lh, lw, 3)
+            valid_o, valid_g = od > 0, gd > 0
+            agree = (valid_o == valid_g).mean()
+            assert agree >= 0.999, (l, agree)
+            both = valid_o & valid_g
+            assert both.sum() > 100
+            err = np.linalg.norm(gv[both] - ov[both], axis=1)
+            assert (err <= 1e-3).mean() >= 0.999, (l, np.percentile(err, 99.9))
+            assert np.percentile(np.abs(gn[both] - on[both]).max(1), 99.9) < 1e-3
+
+
+# ---------------------------------------------------------------------------
+# a6 - a8: ICP on identical inputs (tp_Track_Pose entry point)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("reduce_mode", [V.VS_REDUCE_FP32, V.VS_REDUCE_KAHAN, V.VS_REDUCE_FP64])
+def test_track_pose_identical_inputs(gpu, case, reduce_mode):
+    c = helpers.make_case(width=160, height=120, dim=128, frames=1, seed=3, reduce_mode=reduce_mode)
+    cfg, ocfg = c["cfg"], O.config_from_vs(c["cfg"])
+    vol = O.Volume(ocfg)
+    T0 = case["gt"][1].astype(np.float32)
+    for k in range(2):
+        raw = O.depth_to_m(case["depth"][k])
+        Tgc = case["gt"][k].astype(np.float32)
+        vol.integrate(raw, Tgc, O.pose_inverse(Tgc))
+    t, w = vol.get()
+    with V.Session(cfg) as s:
+        s.set_volume(t, w)
+        s.set_pose(T0.astype(np.float64))
+        Tgc, Tgc64, _ = s.pose()
+        # model maps from the session's own ray cast of the identical volume
+        s.stage_raycast()
+        run_filter(s, case["depth"][2])
+        mv = [s.maps(l)["model_vertex"] for l in range(3)]
+        mn = [s.maps(l)["model_normal"] for l in range(3)]
+        ind = [s.maps(l)["input_depth"] for l in range(3)]
+        ok = s.tp_track_pose()
+        Tg, Tg64, info = s.pose()
+    assert ok
+    # the oracle tracks from the same maps and the same filtered input
+    ook, oT, oinfo = O.track(ocfg, ind, mv, mn, Tgc64, f64=True)
+    assert ook
+    assert helpers.rot_err(Tg64, oT) < 1e-4
+    assert helpers.trans_err(Tg64, oT) < 1e-4
+    # and it moved towards the ground truth of frame 2
+    assert helpers.camera_centre_err(Tg64, case["gt"][2]) < helpers.camera_centre_err(T0, case["gt"][2]) + 2e-3
+
+
+def test_track_pose_singular_system_fails_cleanly(gpu, case):
+    # no model maps yet (fresh session): the 6x6 system is all zeros, the
+    # Cholesky pivot test fails, tracking reports failure and the pose stays
+    with V.Session(case["cfg"]) as s:
+        run_filter(s, case["depth"][0])
+        ok = s.tp_track_pose()
+        T, T64, info = s.pose()
+    assert not ok
+    assert np.array_equal(T64, np.eye(4))
+
+
+# ---------------------------------------------------------------------------
+# end to end (so_Scan_Object hot path)
+# ---------------------------------------------------------------------------
+def test_pipeline_matches_oracle(gpu, case):
+    cfg, ocfg = case["cfg"], case["ocfg"]
+    os_ = O.Session(ocfg)
+    with V.Session(cfg) as s:
+        for k in range(case["depth"].shape[0]):
+            T, tracked = s.scan_frame_host(case["depth"][k])
+            assert tracked
+            assert os_.frame(case["depth"][k])
+            oT = os_.pose()
+            assert helpers.rot_err(T, oT) < 1e-4 * (k + 1), k
+            assert helpers.trans_err(T, oT) < 1e-4 * (k + 1), k
+        m = s.maps(0)
+        om = os_.maps(0)
+        both = (m["model_depth"] > 0) & (om["model_depth"] > 0)
+        assert ((m["model_depth"] > 0) == (om["model_depth"] > 0)).mean() > 0.99
+        err = np.abs(m["model_depth"][both] - om["model_depth"][both])
+        assert (err < 1e-3).mean() > 0.999
+
+
+def test_golden_sequence(gpu):
+    import os
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "seq_small.npz"))
+    c = g["cfg"]
+    cfg = V.default_config(int(c[0]), int(c[1]), fx=float(c[2]), fy=float(c[3]), cx=float(c[4]), cy=float(c[5]),
+                           dim=(int(c[6]),) * 3, origin=(float(c[7]), float(c[8]), float(c[9])),
+                           voxel_size=float(c[10]), mu=float(c[11]), th_icp=float(c[12]))
+    with V.Session(cfg) as s:
+        for k in range(g["depth"].shape[0]):
+            T, tracked = s.scan_frame_host(g["depth"][k])
+            assert tracked
+            assert helpers.rot_err(T, g["poses"][k]) < 1e-4 * (k + 1)
+            assert helpers.trans_err(T, g["poses"][k]) < 1e-4 * (k + 1)
+        t, w = s.volume()
+        md = s.maps(0)["model_depth"]
+    same_w = (w == g["weight"]).mean()
+    assert same_w > 0.995
+    m = (w == g["weight"]) & (w > 0)
+    assert (np.abs(helpers.q16(t[m]) - g["tsdf_q"][m].astype(np.int32)) <= 1).mean() > 0.995
+    both = (md > 0) & (g["model_depth"] > 0)
+    assert (np.abs(md[both] - g["model_depth"][both]) < 1e-3).mean() > 0.999
+
+
+def test_scan_frame_device_input_and_stream(gpu, case):
+    cfg = case["cfg"]
+    with V.Session(cfg) as a, V.Session(cfg) as b:
+        st = torch.cuda.Stream()
+        for k in range(3):
+            d = dev(case["depth"][k].view(np.int16))
+            with torch.cuda.stream(st):
+                b.scan_frame(d.data_ptr(), st.cuda_stream)
+            st.synchronize()
+            Ta, _ = a.scan_frame_host(case["depth"][k])
+        Tb, _, _ = b.pose()
+        assert np.array_equal(Ta, Tb)
+
+
+def test_argument_errors(gpu, case):
+    with V.Session(case["cfg"]) as s:
+        with pytest.raises(V.VsError):
+            s.bfd_bilateral_filter_depth_host(np.zeros((10, 10), np.float32))
+        lib = V.load()
+        assert lib.vs_render_maps(s.h, 5, 5, None, None, None, None, 0, None, None, None, None) == V.VS_ERR_ARG
+        assert lib.vs_integrate_depth(s.h, None, 1, 1, None, None) == V.VS_ERR_ARG

@@ -1,0 +1,215 @@
+// Internal device-side definitions shared by the kernels and the host layer.
+//
+// Arithmetic contract: every translation unit is compiled with -fmad=false,
+// so `a * b + c` is a rounded multiply followed by a rounded add, exactly as
+// the reference's expressions read and as the CPU oracle evaluates them;
+// division and square root are the IEEE-rounded defaults.  Index, weight and
+// int16 TSDF results are therefore bit-identical to the oracle.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "vs.h"
+
+namespace vs {
+
+constexpr int kMaxLevels = 3;
+constexpr int kBrick = 8;             // 8^3 voxels per brick = reference sub-cube
+constexpr int kBrickVox = 512;
+constexpr float kQ = 32767.0f;
+constexpr int kPartials = 32;         // doubles per ICP block partial (29 used)
+constexpr int kIcpMaxBlocks = 304;    // 2 blocks per SM on 152 SMs
+
+struct Level {
+  int W, H;
+  float K[4];  // fx, fy, cx, cy
+};
+
+// Pose and ICP state of one session, device resident.
+struct Pose {
+  double T_gc[16];     // FP64 master pose, global -> camera
+  double T12[16];      // ICP increment of the current frame (camera t0 -> t1)
+  float Tgc[16];       // float copies read by the kernels
+  float Tcg[16];
+  float center[3];     // camera centre in global coordinates
+  float T21[16];       // float inverse of T12, read by the ICP term kernel
+  int level_done[kMaxLevels];
+  int failed;          // 6x6 system singular this frame
+  int skip;            // no tracking this frame (first frame)
+  int iters_run;
+  int valid_count;     // correspondences of the last iteration
+  int frame;           // frames processed
+  int tracked;         // result of the last frame: 1 tracked (or first), 0 lost
+  float last_x[6];
+  double last_sums[29];
+};
+
+// Everything a kernel needs to know about one session, copied to the device
+// once at creation (pointers do not change afterwards).
+struct SessionDev {
+  Level lv[kMaxLevels];
+  int levels;
+  int dim[3];
+  int nb[3];            // bricks per axis
+  float origin[3];
+  float vox, vox_inv, mu, max_w, r_cube;
+  float cube_center[3];
+  float th_icp, cos_normal;
+  int iters[kMaxLevels];
+  int reduce_mode, tsdf_type;
+  float depth_scale;
+  float gauss[5];       // bilateral spatial weights
+  // frame buffers
+  uint16_t* depth_mm;            // level-0 input (uint16)
+  float* depth_raw;              // level-0 metres (integration input)
+  float* depth[kMaxLevels];      // filtered pyramid
+  float4* in_vtx[kMaxLevels];    // input vertex map (w = 1 valid, 0 invalid)
+  float4* in_nrm[kMaxLevels];    // input normal map (w = 1 valid)
+  uint8_t* in_code[kMaxLevels];  // normal-map pre-pass codes
+  uint32_t* in_rmask[kMaxLevels];// per-row rejection bitmasks
+  float* m_depth[kMaxLevels];    // model (ray-cast) maps
+  float4* m_vtx[kMaxLevels];     // xyz, w = 1 valid (invalid: -100)
+  float4* m_nrm[kMaxLevels];
+  uint8_t* m_img[kMaxLevels];
+  // volume
+  void* vol;                     // bricks, 512 words each
+  uint32_t* brick_flag;          // per brick: 1 while listed this frame
+  uint32_t* brick_list;          // active bricks of this frame
+  uint32_t* brick_count;
+  // ICP scratch
+  double* partials;              // [kIcpMaxBlocks][2*kPartials]
+  unsigned* icp_counter;
+  Pose* pose;
+};
+
+// ---------------------------------------------------------------------------
+// small float3 helpers (the reference's ITMMath Vector3f operations)
+// ---------------------------------------------------------------------------
+struct F3 {
+  float x, y, z;
+};
+__host__ __device__ inline F3 f3(float x, float y, float z) { return F3{x, y, z}; }
+__host__ __device__ inline F3 sub(F3 a, F3 b) { return f3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__host__ __device__ inline F3 add(F3 a, F3 b) { return f3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__host__ __device__ inline F3 scale(float s, F3 a) { return f3(s * a.x, s * a.y, s * a.z); }
+__host__ __device__ inline float dot(F3 a, F3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__host__ __device__ inline float length(F3 a) { return sqrtf(dot(a, a)); }
+__host__ __device__ inline F3 normalised(F3 a) {
+  float inv = 1.0f / sqrtf(a.x * a.x + a.y * a.y + a.z * a.z);
+  return f3(a.x * inv, a.y * inv, a.z * inv);
+}
+// d_p_Project (_yooji_cuda_math.h:205-210)
+__host__ __device__ inline void project(F3 p, const float* K, float& u, float& v) {
+  u = K[0] * p.x / p.z + K[2];
+  v = K[1] * p.y / p.z + K[3];
+}
+// d_bp_Back_Project (_yooji_cuda_math.h:212-226)
+__host__ __device__ inline F3 back_project(float u, float v, const float* K, float d) {
+  return f3(d * (u - K[2]) / K[0], d * (v - K[3]) / K[1], d);
+}
+// d_t_Transform / d_r_Rotate (_yooji_cuda_math.h:229-244)
+__host__ __device__ inline F3 transform(F3 p, const float* M) {
+  return f3(M[0] * p.x + M[1] * p.y + M[2] * p.z + M[3], M[4] * p.x + M[5] * p.y + M[6] * p.z + M[7],
+            M[8] * p.x + M[9] * p.y + M[10] * p.z + M[11]);
+}
+__host__ __device__ inline F3 rotate(F3 p, const float* M) {
+  return f3(M[0] * p.x + M[1] * p.y + M[2] * p.z, M[4] * p.x + M[5] * p.y + M[6] * p.z,
+            M[8] * p.x + M[9] * p.y + M[10] * p.z);
+}
+// ROUNDF (_yooji_cuda_defines.h): half away from zero via truncation
+__host__ __device__ inline int roundf_ref(float x) {
+  return (x < 0.0f) ? (int)(x - 0.5f) : (int)(x + 0.5f);
+}
+// d_gpv_Get_Position_in_Voxel (_yooji_cuda_math.h:265-283)
+__device__ inline bool pos_in_voxel(F3 p, const SessionDev& s, F3& v) {
+  v.x = (p.x - s.origin[0]) * s.vox_inv - 0.5f;
+  v.y = (p.y - s.origin[1]) * s.vox_inv - 0.5f;
+  v.z = (p.z - s.origin[2]) * s.vox_inv - 0.5f;
+  return !(v.x < -0.5f || v.x >= (float)s.dim[0] - 0.5f || v.y < -0.5f ||
+           v.y >= (float)s.dim[1] - 0.5f || v.z < -0.5f || v.z >= (float)s.dim[2] - 0.5f);
+}
+// d_gpw_Get_Position_in_World (_yooji_cuda_math.h:285-302)
+__device__ inline F3 pos_in_world(F3 v, const SessionDev& s) {
+  return f3((v.x + 0.5f) / s.vox_inv + s.origin[0], (v.y + 0.5f) / s.vox_inv + s.origin[1],
+            (v.z + 0.5f) / s.vox_inv + s.origin[2]);
+}
+
+// ---------------------------------------------------------------------------
+// voxel storage
+//   INT16: word = (uint16 weight << 16) | uint16(int16 q), tsdf = q / 32767
+//   FP16 : word = (uint16 weight << 16) | half bits
+//   FP32 : uint2 {float bits, uint32 weight}
+// Bricks are 512 consecutive words, x fastest inside the brick; bricks are
+// ordered x fastest, then y, then z.
+// ---------------------------------------------------------------------------
+__host__ __device__ inline size_t brick_word_index(int x, int y, int z, const int* nb) {
+  size_t b = ((size_t)(z >> 3) * nb[1] + (size_t)(y >> 3)) * nb[0] + (size_t)(x >> 3);
+  return b * kBrickVox + (size_t)(((z & 7) << 6) | ((y & 7) << 3) | (x & 7));
+}
+
+__device__ inline float q_to_tsdf(int q) { return (float)q * (1.0f / kQ); }
+__device__ inline int tsdf_to_q(float t) {
+  float r = rintf(t * kQ);
+  r = fminf(fmaxf(r, -kQ), kQ);
+  return (int)r;
+}
+
+struct StoreI16 {
+  typedef uint32_t word;
+  __device__ static inline void decode(word v, float& t, uint32_t& w) {
+    t = q_to_tsdf((int)(int16_t)(v & 0xffffu));
+    w = v >> 16;
+  }
+  __device__ static inline word encode(float t, uint32_t w) {
+    return (w << 16) | ((uint32_t)(uint16_t)(int16_t)tsdf_to_q(t));
+  }
+  __device__ static inline word initial() { return (uint32_t)(uint16_t)(int16_t)32767; }
+};
+struct StoreF16 {
+  typedef uint32_t word;
+  __device__ static inline void decode(word v, float& t, uint32_t& w) {
+    t = __half2float(__ushort_as_half((unsigned short)(v & 0xffffu)));
+    w = v >> 16;
+  }
+  __device__ static inline word encode(float t, uint32_t w) {
+    return (w << 16) | (uint32_t)__half_as_ushort(__float2half_rn(t));
+  }
+  __device__ static inline word initial() { return (uint32_t)__half_as_ushort(__float2half_rn(1.0f)); }
+};
+struct StoreF32 {
+  typedef uint2 word;
+  __device__ static inline void decode(word v, float& t, uint32_t& w) {
+    t = __uint_as_float(v.x);
+    w = v.y;
+  }
+  __device__ static inline word encode(float t, uint32_t w) { return make_uint2(__float_as_uint(t), w); }
+  __device__ static inline word initial() { return make_uint2(__float_as_uint(1.0f), 0u); }
+};
+
+inline size_t voxel_bytes(int tsdf_type) { return tsdf_type == VS_TSDF_FP32 ? 8 : 4; }
+
+// ---------------------------------------------------------------------------
+// launch wrappers (one per kernel file)
+// ---------------------------------------------------------------------------
+void launch_filter(const SessionDev* d, const SessionDev& h, cudaStream_t st);
+void launch_input_maps(const SessionDev* d, const SessionDev& h, cudaStream_t st);
+void launch_bilateral_float(const SessionDev* d, const SessionDev& h, const float* in, float* out,
+                            cudaStream_t st);
+void launch_icp(const SessionDev* d, const SessionDev& h, cudaStream_t st, bool frame_mode,
+                const float* init_T12_dev);
+void launch_integrate(const SessionDev* d, const SessionDev& h, const float* depth,
+                      const float* Tgc, const float* Tcg, bool gate_on_tracking, cudaStream_t st);
+void launch_raycast(const SessionDev* d, const SessionDev& h, int level_begin, int level_end,
+                    const float* Tgc, const float* Tcg, const float* center, float lx, float ly,
+                    float lz, bool gate_on_tracking, float* out_depth, float* out_vtx3,
+                    float* out_nrm3, uint8_t* out_img, cudaStream_t st);
+void launch_volume_init(const SessionDev& h, cudaStream_t st);
+void launch_volume_export(const SessionDev& h, float* tsdf, uint16_t* w, cudaStream_t st);
+void launch_volume_import(const SessionDev& h, const float* tsdf, const uint16_t* w,
+                          cudaStream_t st);
+void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
+void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3,
+                        float* inrm3, cudaStream_t st);
+
+}  // namespace vs
