@@ -399,7 +399,9 @@ void point_normal_map(const T* depth, int w, int h, const T* K, T* vtx, T* nrm) 
 // ---------------------------------------------------------------------------
 template <class T>
 inline bool bilinear3(T xf, T yf, int w, int h, const float* map, V3<T>& out) {
-  if (xf < T(0) || xf > T(w - 1) || yf < T(0) || yf > T(h - 1)) return false;
+  // NaN coordinates (a point at z = 0) are rejected; the reference leaves
+  // them to an undefined float-to-int conversion
+  if (!(xf >= T(0) && xf <= T(w - 1) && yf >= T(0) && yf <= T(h - 1))) return false;
   int x = (int)xf, y = (int)yf;
   T rx = xf - (T)x, ry = yf - (T)y;
   V3<T> a{0, 0, 0}, b{0, 0, 0}, c{0, 0, 0}, d{0, 0, 0};
@@ -853,6 +855,7 @@ void update_tsdf(Volume<T>& V, const float* depth, const T* T_gc, const T* T_cg)
 template <class T>
 inline bool gtvu(const Volume<T>& V, V3<T> p, T& out) {
   out = T(1);
+  if (std::isnan(p.x) || std::isnan(p.y) || std::isnan(p.z)) return false;
   int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
   const int* d = V.g.dim;
   if (x < 0 || x >= d[0] || y < 0 || y >= d[1] || z < 0 || z >= d[2]) return false;
@@ -875,6 +878,7 @@ inline void to_int_floor(V3<T> p, int o[3], V3<T>& r) {
 template <class T>
 inline bool gtvi(const Volume<T>& V, V3<T> p, T& out) {
   out = T(1);
+  if (std::isnan(p.x) || std::isnan(p.y) || std::isnan(p.z)) return false;
   int o[3];
   V3<T> r;
   to_int_floor(p, o, r);
@@ -895,6 +899,7 @@ bool surface_normal(const Volume<T>& V, V3<T> p3d, V3<T>& nout) {
   const Cfg<T>& g = V.g;
   V3<T> vox;
   if (!pos_in_voxel(p3d, g.origin, g.dim, g.vox_inv, vox)) return false;
+  if (std::isnan(vox.x) || std::isnan(vox.y) || std::isnan(vox.z)) return false;
   int o[3];
   V3<T> r;
   to_int_floor(vox, o, r);

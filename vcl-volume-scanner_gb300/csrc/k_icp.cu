@@ -30,7 +30,8 @@ namespace {
 constexpr int kThreads = 256;
 
 __device__ inline bool bilinear4(float xf, float yf, int w, int h, const float4* __restrict__ map, F3& out) {
-  if (xf < 0.0f || xf > (float)(w - 1) || yf < 0.0f || yf > (float)(h - 1)) return false;
+  // NaN coordinates are rejected (see the oracle)
+  if (!(xf >= 0.0f && xf <= (float)(w - 1) && yf >= 0.0f && yf <= (float)(h - 1))) return false;
   int x = (int)xf, y = (int)yf;
   float rx = xf - (float)x, ry = yf - (float)y;
   F3 a = f3(0, 0, 0), b = f3(0, 0, 0), c = f3(0, 0, 0), d = f3(0, 0, 0);

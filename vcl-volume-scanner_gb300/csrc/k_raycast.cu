@@ -48,6 +48,7 @@ struct Vol {
   // d_gtvu_Get_TSDF_Value_Uninterpolated: nearest voxel (ROUNDF), weight > 0
   __device__ inline bool gtvu(F3 p, float& out) const {
     out = 1.0f;
+    if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return false;
     int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
     if (x < 0 || x >= dim[0] || y < 0 || y >= dim[1] || z < 0 || z >= dim[2]) return false;
     float t;
@@ -69,6 +70,7 @@ struct Vol {
   // d_gtvi_Get_TSDF_Value_Interpolated (offset = floor, see the oracle)
   __device__ inline bool gtvi(F3 p, float& out) const {
     out = 1.0f;
+    if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return false;
     float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
     int ox = (int)fx, oy = (int)fy, oz = (int)fz;
     float rx = p.x - fx, ry = p.y - fy, rz = p.z - fz;
@@ -91,6 +93,7 @@ template <class S>
 __device__ bool surface_normal(const Vol<S>& V, const SessionDev& s, F3 p3d, F3& nout) {
   F3 vox;
   if (!pos_in_voxel(p3d, s, vox)) return false;
+  if (isnan(vox.x) || isnan(vox.y) || isnan(vox.z)) return false;
   float fx = floorf(vox.x), fy = floorf(vox.y), fz = floorf(vox.z);
   const int ox = (int)fx, oy = (int)fy, oz = (int)fz;
   const float rx = vox.x - fx, ry = vox.y - fy, rz = vox.z - fz;
