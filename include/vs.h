@@ -170,6 +170,22 @@ int vs_get_active_bricks(vs_session* s, uint32_t* count, uint32_t* bricks_host,
 int vs_get_maps(vs_session* s, int level, float* model_depth, float* model_vertex3,
                 float* model_normal3, uint8_t* model_img, float* input_depth,
                 float* input_vertex3, float* input_normal3);
+/* ---- instrumentation (the reference prints per-stage stopwatch times,
+ * z_yooji_object_scanner.cpp:489-604) ------------------------------------- */
+
+/* records CUDA events between the stages of the per-frame graph (the graph is
+ * re-captured on the next frame) */
+int vs_set_stage_timing(vs_session* s, int enable);
+/* device milliseconds of the last frame: filter (ingest, bilateral, pyramid,
+ * input maps), track, integrate, ray-cast; waits for the frame */
+int vs_get_stage_times(vs_session* s, float* ms4);
+/* counters of the last frame: [0] active sub-cubes, [1] voxels updated,
+ * [2] ICP iterations run, [3] correspondences of the last iteration */
+int vs_get_frame_stats(vs_session* s, uint32_t* stats4);
+/* kernel launches one vs_scan_frame performs for this configuration (-1 if
+ * the configuration is invalid) */
+int vs_kernels_per_frame(const vs_config* cfg);
+
 /* level-0 depth in metres as converted from the last uint16 input frame (the
  * integration input, musf_Matrix_Ushort_to_Float with the depth scale,
  * z_yooji_frame_capture.cpp:597) */

@@ -26,11 +26,13 @@ def _newer(out, srcs):
 
 
 def build_oracle(force=False):
+    """OpenMP parallelises the per-pixel / per-sub-cube loops only; every
+    result is independent of the thread count (OMP_NUM_THREADS)."""
     out = os.path.join(HERE, "_build", "liboracle.so")
     srcs = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle.h")]
     if force or not _newer(out, srcs):
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        subprocess.check_call([CXX] + FLAGS + ["-o", out, srcs[0]])
+        subprocess.check_call([CXX] + FLAGS + ["-fopenmp", "-o", out, srcs[0]])
     return out
 
 

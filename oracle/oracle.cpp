@@ -287,6 +287,7 @@ void bilateral(const T* in, int w, int h, T* out) {
   T g[5];
   gaussian_table<T>((T)4.0f, r, g);
   const T denom = T(2) * e_d * e_d;
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < h; y++) {
     for (int x = 0; x < w; x++) {
       T sum = 0, t = 0;
@@ -320,11 +321,13 @@ template <class T>
 void pyramid_down(const T* in, int w, int h, T* out) {
   std::vector<T> pad((size_t)w * h, T(0)), sm((size_t)w * h, T(0));
   const T f0 = 1, f1 = 4, f2 = 6;
+#pragma omp parallel for schedule(static)
   for (int j = 0; j < h; j++)
     for (int i = 2; i < w - 2; i++) {
       const T* p = in + (size_t)j * w;
       pad[(size_t)j * w + i] = f0 * p[i - 2] + f0 * p[i + 2] + f1 * p[i - 1] + f1 * p[i + 1] + f2 * p[i];
     }
+#pragma omp parallel for schedule(static)
   for (int i = 2; i < w - 2; i++)
     for (int j = 2; j < h - 2; j++) {
       const T* p = pad.data() + i;
@@ -350,6 +353,7 @@ template <class T>
 void point_normal_map(const T* depth, int w, int h, const T* K, T* vtx, T* nrm) {
   size_t n = (size_t)w * h;
   for (size_t k = 0; k < 3 * n; k++) vtx[k] = nrm[k] = T(-100);
+#pragma omp parallel for schedule(static)
   for (int i = 0; i < h; i++)
     for (int j = 0; j < w; j++) {
       size_t t = (size_t)i * w + j;
@@ -495,11 +499,13 @@ void icp_sums(const Cfg<T>& g, int lev, const float* depth, const float* mvtx, c
   };
   if (mode == 0) {
     int gx = (w + 15) / 16, gy = (h + 15) / 16;
-    T host[29];
-    for (int k = 0; k < 29; k++) host[k] = 0;
-    std::vector<T> cache((size_t)256 * 29);
-    for (int by = 0; by < gy; by++)
-      for (int bx = 0; bx < gx; bx++) {
+    std::vector<T> part((size_t)gx * gy * 29);
+#pragma omp parallel
+    {
+      std::vector<T> cache((size_t)256 * 29);
+#pragma omp for schedule(static)
+      for (int bidx = 0; bidx < gx * gy; bidx++) {
+        int bx = bidx % gx, by = bidx / gx;
         for (int ty = 0; ty < 16; ty++)
           for (int tx = 0; tx < 16; tx++) {
             int x = bx * 16 + tx, y = by * 16 + ty, cidx = tx + ty * 16;
@@ -511,8 +517,13 @@ void icp_sums(const Cfg<T>& g, int lev, const float* depth, const float* mvtx, c
         for (int i = 128; i != 0; i /= 2)
           for (int c = 0; c < i; c++)
             for (int k = 0; k < 29; k++) cache[(size_t)c * 29 + k] += cache[(size_t)(c + i) * 29 + k];
-        for (int k = 0; k < 29; k++) host[k] += cache[k];
+        for (int k = 0; k < 29; k++) part[(size_t)bidx * 29 + k] = cache[k];
       }
+    }
+    T host[29];
+    for (int k = 0; k < 29; k++) host[k] = 0;
+    for (int bidx = 0; bidx < gx * gy; bidx++)
+      for (int k = 0; k < 29; k++) host[k] += part[(size_t)bidx * 29 + k];
     for (int k = 0; k < 29; k++) out29[k] = (double)host[k];
     return;
   }
@@ -786,6 +797,7 @@ void find_visible_subcubes(Volume<T>& V, const float* depth, const T* T_cg) {
   const int w = g.W[0], h = g.H[0];
   const T* K = g.K[0];
   std::fill(V.flags.begin(), V.flags.end(), 0);
+#pragma omp parallel for schedule(static)
   for (int ty = 0; ty < h; ty++)
     for (int tx = 0; tx < w; tx++) {
       T td = (T)depth[(size_t)ty * w + tx];
@@ -799,7 +811,9 @@ void find_visible_subcubes(Volume<T>& V, const float* depth, const T* T_cg) {
         if (!pos_in_voxel(tp, g.origin, g.dim, g.vox_inv, vox)) continue;
         int xs = roundf_div_ref(vox.x, 8), ys = roundf_div_ref(vox.y, 8), zs = roundf_div_ref(vox.z, 8);
         if (xs < 0 || xs >= V.nsc[0] || ys < 0 || ys >= V.nsc[1] || zs < 0 || zs >= V.nsc[2]) break;
-        V.flags[((size_t)zs * V.nsc[1] + ys) * V.nsc[0] + xs] = 1;
+        uint8_t& f = V.flags[((size_t)zs * V.nsc[1] + ys) * V.nsc[0] + xs];
+#pragma omp atomic write
+        f = 1;
       }
     }
 }
@@ -813,10 +827,11 @@ void update_tsdf(Volume<T>& V, const float* depth, const T* T_gc, const T* T_cg)
   const int w = g.W[0], h = g.H[0];
   const T* K = g.K[0];
   const int X = g.dim[0], Y = g.dim[1];
-  for (int zs = 0; zs < V.nsc[2]; zs++)
-    for (int ys = 0; ys < V.nsc[1]; ys++)
-      for (int xs = 0; xs < V.nsc[0]; xs++) {
-        if (!V.flags[((size_t)zs * V.nsc[1] + ys) * V.nsc[0] + xs]) continue;
+  const int nsc = V.nsc[0] * V.nsc[1] * V.nsc[2];
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int sc = 0; sc < nsc; sc++) {
+    const int xs = sc % V.nsc[0], ys = (sc / V.nsc[0]) % V.nsc[1], zs = sc / (V.nsc[0] * V.nsc[1]);
+        if (!V.flags[sc]) continue;
         for (int lz = 0; lz < 8; lz++)
           for (int ly = 0; ly < 8; ly++)
             for (int lx = 0; lx < 8; lx++) {
@@ -1042,6 +1057,7 @@ void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> ca
   V3<T> ncc = normalised(vcc);
   T dist_cc = length(vcc);
   T theta_max = std::asin(g.r_cube / dist_cc);
+#pragma omp parallel for schedule(dynamic, 4)
   for (int ty = 0; ty < h; ty++)
     for (int tx = 0; tx < w; tx++) {
       size_t t = (size_t)ty * w + tx;

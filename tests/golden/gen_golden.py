@@ -8,10 +8,10 @@ refpin.npz
     reference tree by oracle/build_oracle.py.  These pin the oracle's pose
     algebra bit for bit.
 seq_small.npz
-    A 6-frame 80x60 synthetic sequence (uint16 input frames stored, so no
+    A 6-frame 160x120 synthetic sequence (uint16 input frames stored, so no
     cross-host generator identity is assumed) and the oracle's outputs for it
-    (64^3 int16 volume): per-frame poses, final weights / quantised TSDF, and
-    the level-0 model depth of the last frame.
+    (96^3 int16 volume over 0.75 m): per-frame poses and tracking flags, final
+    weights / quantised TSDF, and the level-0 model depth of the last frame.
 """
 import ctypes
 import os
@@ -57,19 +57,22 @@ def refpin():
 
 def seq_small():
     import helpers
-    case = helpers.make_case(width=80, height=60, dim=64, frames=6, seed=11, size=1.0)
+    case = helpers.make_case(width=160, height=120, dim=96, frames=6, seed=11, size=0.75)
     depth, ocfg = case["depth"], case["ocfg"]
     s = O.Session(ocfg)
     poses = []
+    tracked = []
     for k in range(depth.shape[0]):
-        s.frame(depth[k])
+        tracked.append(s.frame(depth[k]))
         poses.append(s.pose())
+    assert all(tracked)
     t, w = s.volume().get()
     m = s.maps(0)
     c = case["cfg"]
     cfg_arr = np.array([c.width, c.height, c.fx, c.fy, c.cx, c.cy, c.dim[0], c.origin[0], c.origin[1], c.origin[2],
                         c.voxel_size, c.mu, c.th_icp], np.float64)
-    np.savez_compressed(os.path.join(OUT, "seq_small.npz"), depth=depth, poses=np.array(poses), weight=w,
+    np.savez_compressed(os.path.join(OUT, "seq_small.npz"), depth=depth, poses=np.array(poses),
+                        tracked=np.array(tracked), weight=w,
                         tsdf_q=helpers.q16(t).astype(np.int16), model_depth=m["model_depth"], cfg=cfg_arr,
                         gt=case["gt"])
 

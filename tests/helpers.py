@@ -24,9 +24,13 @@ def make_case(width=160, height=120, dim=128, size=1.0, frames=4, seed=3, f_ref=
 
 
 def rot_err(A, B):
-    """rotation angle (rad) of A^T B for 4x4 or 3x3 poses"""
+    """rotation angle (rad) of A^T B for 4x4 or 3x3 poses; atan2 of the skew
+    and symmetric parts, which stays accurate for tiny angles (arccos of the
+    trace does not: a float rotation's own orthogonality error would read as
+    ~1e-4 rad)"""
     R = np.asarray(A, np.float64)[:3, :3].T @ np.asarray(B, np.float64)[:3, :3]
-    return float(np.arccos(np.clip((np.trace(R) - 1.0) / 2.0, -1.0, 1.0)))
+    w = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / 2.0
+    return float(np.arctan2(np.linalg.norm(w), (np.trace(R) - 1.0) / 2.0))
 
 
 def trans_err(A, B):

@@ -219,11 +219,15 @@ def test_track_pose_identical_inputs(gpu, case, reduce_mode):
         ok = s.tp_track_pose()
         Tg, Tg64, info = s.pose()
     assert ok
-    # the oracle tracks from the same maps and the same filtered input
-    ook, oT, oinfo = O.track(ocfg, ind, mv, mn, Tgc64, f64=True)
+    # the oracle tracks from the same maps and the same filtered input, with
+    # the same float per-pixel terms (its solve is the reference's FP32 one)
+    ook, oT, oinfo = O.track(ocfg, ind, mv, mn, Tgc, f64=False)
     assert ook
     assert helpers.rot_err(Tg64, oT) < 1e-4
     assert helpers.trans_err(Tg64, oT) < 1e-4
+    # and the FP64 oracle (double per-pixel terms) agrees as well
+    dok, dT, _ = O.track(ocfg, ind, mv, mn, Tgc64, f64=True)
+    assert dok and helpers.rot_err(Tg64, dT) < 1e-4 and helpers.trans_err(Tg64, dT) < 1e-4
     # and it moved towards the ground truth of frame 2
     assert helpers.camera_centre_err(Tg64, case["gt"][2]) < helpers.camera_centre_err(T0, case["gt"][2]) + 2e-3
 
@@ -251,6 +255,7 @@ def test_pipeline_matches_oracle(gpu, case):
             assert tracked
             assert os_.frame(case["depth"][k])
             oT = os_.pose()
+            # per-frame tolerance, allowed to add up over the frames
             assert helpers.rot_err(T, oT) < 1e-4 * (k + 1), k
             assert helpers.trans_err(T, oT) < 1e-4 * (k + 1), k
         m = s.maps(0)
@@ -271,7 +276,7 @@ def test_golden_sequence(gpu):
     with V.Session(cfg) as s:
         for k in range(g["depth"].shape[0]):
             T, tracked = s.scan_frame_host(g["depth"][k])
-            assert tracked
+            assert tracked == bool(g["tracked"][k])
             assert helpers.rot_err(T, g["poses"][k]) < 1e-4 * (k + 1)
             assert helpers.trans_err(T, g["poses"][k]) < 1e-4 * (k + 1)
         t, w = s.volume()

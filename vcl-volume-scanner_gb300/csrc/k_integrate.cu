@@ -102,6 +102,7 @@ __global__ void __launch_bounds__(kIntThreads)
 
   for (uint32_t i = gwarp; i < count; i += nwarps) {
     const uint32_t b = s->brick_list[i];
+    int nupd = 0;
     const int bx = (int)(b % (uint32_t)nb0), by = (int)((b / (uint32_t)nb0) % (uint32_t)nb1),
               bz = (int)(b / ((uint32_t)nb0 * (uint32_t)nb1));
     uint4* bv = reinterpret_cast<uint4*>(vol + (size_t)b * kBrickVox);
@@ -141,13 +142,19 @@ __global__ void __launch_bounds__(kIntThreads)
         float tnew = (oldW * told + ts) * inewW;
         wv[e] = S::encode(tnew, (uint32_t)newW);
         changed = true;
+        nupd++;
       }
       if (changed) {
         memcpy(&raw, wv, 16);
         bv[vi] = raw;
       }
     }
-    if (lane == 0) s->brick_flag[b] = 0u;
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
+    if (lane == 0) {
+      s->brick_flag[b] = 0u;
+      if (nupd) atomicAdd(s->brick_count + 1, (uint32_t)nupd);
+    }
   }
 }
 
@@ -206,7 +213,7 @@ int sm_count() {
 
 void launch_integrate(const SessionDev* d, const SessionDev& h, const float* depth, const float* Tgc,
                       const float* Tcg, bool gate, cudaStream_t st) {
-  cudaMemsetAsync(h.brick_count, 0, sizeof(uint32_t), st);
+  cudaMemsetAsync(h.brick_count, 0, 2 * sizeof(uint32_t), st);
   dim3 b(32, 8), g((h.lv[0].W + 31) / 32, (h.lv[0].H + 7) / 8);
   k_activate<<<g, b, 0, st>>>(d, depth, Tcg, gate ? 1 : 0);
   // persistent grid: enough warps to cover every SM several times over

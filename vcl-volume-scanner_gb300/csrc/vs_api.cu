@@ -43,6 +43,8 @@ struct vs_session {
   float* dev_small = nullptr;    // 16 floats of scratch (camera centre)
   Pose* host_pose = nullptr;     // pinned
   int device = 0;
+  bool timing = false;           // stage events recorded inside the graph
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
 namespace {
@@ -148,6 +150,8 @@ size_t volume_bytes(const vs_config* c) {
 }
 
 void free_all(vs_session* s) {
+  for (auto& e : s->ev)
+    if (e) cudaEventDestroy(e), e = nullptr;
   if (s->exec) cudaGraphExecDestroy(s->exec);
   if (s->graph) cudaGraphDestroy(s->graph);
   s->exec = nullptr;
@@ -200,15 +204,24 @@ const float* pose_field(const SessionDev& h, size_t off) {
 #define POSE_TCG(h) pose_field(h, offsetof(Pose, Tcg))
 #define POSE_CEN(h) pose_field(h, offsetof(Pose, center))
 
-// the per-frame sequence (recorded into the graph)
+// the per-frame sequence (recorded into the graph); with stage timing on,
+// event-record nodes separate filter / track / integrate / ray-cast
 void record_frame(vs_session* s, cudaStream_t st) {
   const SessionDev& h = s->h;
+  auto mark = [&](int i) {
+    if (s->timing) cudaEventRecordWithFlags(s->ev[i], st, cudaEventRecordExternal);
+  };
+  mark(0);
   launch_filter(s->d, h, st);
   if (h.cos_normal > -2.0f) launch_input_maps(s->d, h, st);
+  mark(1);
   launch_icp(s->d, h, st, true, nullptr);
+  mark(2);
   launch_integrate(s->d, h, h.depth_raw, POSE_TGC(h), POSE_TCG(h), true, st);
+  mark(3);
   launch_raycast(s->d, h, 0, h.levels, POSE_TGC(h), POSE_TCG(h), POSE_CEN(h), 0.0f, 0.0f, -1.0f, true, nullptr,
                  nullptr, nullptr, nullptr, st);
+  mark(4);
 }
 
 int build_graph(vs_session* s) {
@@ -452,7 +465,7 @@ int vs_scan_frame_host(vs_session* s, const uint16_t* depth_mm_host, float* T_gc
   const size_t n0 = (size_t)s->h.lv[0].W * s->h.lv[0].H;
   VS_CU(cudaMemcpyAsync(s->h.depth_mm, depth_mm_host, n0 * 2, cudaMemcpyHostToDevice, s->stream));
   VS_CU(cudaGraphLaunch(s->exec, s->stream));
-  VS_CU(cudaMemcpyAsync(s->host_pose, s->h.pose, sizeof(Pose), cudaMemcpyDeviceToHost, s->stream));
+  VS_CU(cudaMemcpyAsync(s->host_pose, s->h.pose, kPoseHeadBytes, cudaMemcpyDeviceToHost, s->stream));
   VS_CU(cudaStreamSynchronize(s->stream));
   if (T_gc_out) std::memcpy(T_gc_out, s->host_pose->Tgc, 16 * sizeof(float));
   if (tracked) *tracked = s->host_pose->tracked;
@@ -607,6 +620,53 @@ int vs_get_maps(vs_session* s, int level, float* mdepth, float* mvtx3, float* mn
     if (e != cudaSuccess) return cuda_fail(e, "vs_get_maps");
   }
   return VS_OK;
+}
+
+int vs_set_stage_timing(vs_session* s, int enable) {
+  if (!s) return fail(VS_ERR_ARG, "null session");
+  VS_CU(cudaStreamSynchronize(s->stream));
+  if (enable && !s->ev[0])
+    for (auto& e : s->ev) VS_CU(cudaEventCreate(&e));
+  if ((enable != 0) != s->timing) {
+    s->timing = enable != 0;
+    if (s->exec) cudaGraphExecDestroy(s->exec);
+    if (s->graph) cudaGraphDestroy(s->graph);
+    s->exec = nullptr;
+    s->graph = nullptr;
+  }
+  return VS_OK;
+}
+
+int vs_get_stage_times(vs_session* s, float* ms) {
+  if (!s || !ms) return fail(VS_ERR_ARG, "null argument");
+  if (!s->timing) return fail(VS_ERR_STATE, "stage timing is off");
+  VS_CU(cudaEventSynchronize(s->ev[4]));
+  for (int i = 0; i < 4; i++) VS_CU(cudaEventElapsedTime(ms + i, s->ev[i], s->ev[i + 1]));
+  return VS_OK;
+}
+
+int vs_get_frame_stats(vs_session* s, uint32_t* stats) {
+  if (!s || !stats) return fail(VS_ERR_ARG, "null argument");
+  uint32_t c[2] = {0, 0};
+  VS_CU(cudaMemcpyAsync(c, s->h.brick_count, sizeof(c), cudaMemcpyDeviceToHost, s->stream));
+  VS_CU(cudaMemcpyAsync(s->host_pose, s->h.pose, kPoseHeadBytes, cudaMemcpyDeviceToHost, s->stream));
+  VS_CU(cudaStreamSynchronize(s->stream));
+  stats[0] = c[0];
+  stats[1] = c[1];
+  stats[2] = (uint32_t)s->host_pose->iters_run;
+  stats[3] = (uint32_t)s->host_pose->valid_count;
+  return VS_OK;
+}
+
+int vs_kernels_per_frame(const vs_config* c) {
+  if (check_config(c) != VS_OK) return -1;
+  int n = 1 + (c->levels - 1);              // bilateral + pyramid levels
+  if (c->cos_normal > -2.0f) n += 3;        // input maps: pre, row scan, post
+  n += 2;                                   // ICP begin / finish
+  for (int l = 0; l < c->levels; l++) n += c->icp_iters[l];
+  n += 2;                                   // activation + update
+  n += 1;                                   // ray-cast of every level
+  return n;
 }
 
 int vs_get_input_raw(vs_session* s, float* depth_m_host) {

@@ -26,24 +26,26 @@ struct Level {
   float K[4];  // fx, fy, cx, cy
 };
 
-// Pose and ICP state of one session, device resident.
+// Pose and ICP state of one session, device resident.  The first 80 bytes
+// (float pose and frame result) are what the host reads back per frame.
 struct Pose {
-  double T_gc[16];     // FP64 master pose, global -> camera
-  double T12[16];      // ICP increment of the current frame (camera t0 -> t1)
   float Tgc[16];       // float copies read by the kernels
-  float Tcg[16];
-  float center[3];     // camera centre in global coordinates
-  float T21[16];       // float inverse of T12, read by the ICP term kernel
-  int level_done[kMaxLevels];
-  int failed;          // 6x6 system singular this frame
-  int skip;            // no tracking this frame (first frame)
+  int tracked;         // result of the last frame: 1 tracked (or first), 0 lost
   int iters_run;
   int valid_count;     // correspondences of the last iteration
   int frame;           // frames processed
-  int tracked;         // result of the last frame: 1 tracked (or first), 0 lost
+  float Tcg[16];
+  float center[3];     // camera centre in global coordinates
+  float T21[16];       // float inverse of T12, read by the ICP term kernel
+  double T_gc[16];     // FP64 master pose, global -> camera
+  double T12[16];      // ICP increment of the current frame (camera t0 -> t1)
+  int level_done[kMaxLevels];
+  int failed;          // 6x6 system singular this frame
+  int skip;            // no tracking this frame (first frame)
   float last_x[6];
   double last_sums[29];
 };
+constexpr size_t kPoseHeadBytes = 80;
 
 // Everything a kernel needs to know about one session, copied to the device
 // once at creation (pointers do not change afterwards).
@@ -76,7 +78,7 @@ struct SessionDev {
   void* vol;                     // bricks, 512 words each
   uint32_t* brick_flag;          // per brick: 1 while listed this frame
   uint32_t* brick_list;          // active bricks of this frame
-  uint32_t* brick_count;
+  uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame)
   // ICP scratch
   double* partials;              // [kIcpMaxBlocks][2*kPartials]
   unsigned* icp_counter;

@@ -107,6 +107,10 @@ _SIGS = {
     "vs_set_volume": (_I, [_P, _P, _P]),
     "vs_get_active_bricks": (_I, [_P, ctypes.POINTER(ctypes.c_uint32), _P, ctypes.c_uint32]),
     "vs_get_maps": (_I, [_P, _I, _P, _P, _P, _P, _P, _P, _P]),
+    "vs_set_stage_timing": (_I, [_P, _I]),
+    "vs_get_stage_times": (_I, [_P, _P]),
+    "vs_get_frame_stats": (_I, [_P, _P]),
+    "vs_kernels_per_frame": (_I, [ctypes.POINTER(VsConfig)]),
     "vs_get_input_raw": (_I, [_P, _P]),
     "vs_get_device_buffer": (_I, [_P, _I, ctypes.POINTER(_P)]),
 }
@@ -313,6 +317,24 @@ class Session:
         return dict(model_depth=md.reshape(h, w), model_vertex=mv.reshape(h, w, 3), model_normal=mn.reshape(h, w, 3),
                     model_img=mi.reshape(h, w), input_depth=idp.reshape(h, w), input_vertex=iv.reshape(h, w, 3),
                     input_normal=inn.reshape(h, w, 3))
+
+    def set_stage_timing(self, enable=True):
+        _check(self.lib.vs_set_stage_timing(self.h, 1 if enable else 0))
+
+    def stage_times(self):
+        """device ms of the last frame: filter, track, integrate, ray-cast"""
+        ms = np.empty(4, np.float32)
+        _check(self.lib.vs_get_stage_times(self.h, _ptr(ms)))
+        return ms
+
+    def frame_stats(self):
+        """active sub-cubes, voxels updated, ICP iterations, correspondences"""
+        st = np.empty(4, np.uint32)
+        _check(self.lib.vs_get_frame_stats(self.h, _ptr(st)))
+        return st
+
+    def kernels_per_frame(self):
+        return self.lib.vs_kernels_per_frame(ctypes.byref(self.cfg))
 
     def input_raw(self):
         out = np.empty((self.cfg.height, self.cfg.width), np.float32)
