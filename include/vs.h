@@ -194,6 +194,30 @@ int vs_get_input_raw(vs_session* s, float* depth_m_host);
  * which = 0 raw depth (float m, level 0), 1..3 filtered depth levels 0..2 */
 int vs_get_device_buffer(vs_session* s, int which, void** ptr);
 
+/* ---- allocation-free integration ----------------------------------------
+ * No counterpart in the reference.  For callers that cannot call cudaMalloc
+ * (code running inside a host framework's own device-memory pool or arena,
+ * real-time loops that cannot afford an allocation's driver lock, processes
+ * that size all device memory up front): the same TSDF update as
+ * vs_integrate_depth, into a volume buffer the caller owns, with no device
+ * allocation by this library.  Scratch is a fixed ~2 MiB __device__ array
+ * inside the library (held by every GPU that loads it until exit), which caps
+ * the volume at 262,144 sub-cubes (512^3 voxels); larger volumes return
+ * VS_ERR_ARG.  The first call on a device looks up the scratch address
+ * (cudaGetSymbolAddress) and should come before any stream capture.  Calls
+ * share the scratch: calls on one stream run in order, calls that overlap on
+ * the GPU race.  Asynchronous on `stream` (cudaStream_t, NULL = default).
+ *   volume_dev: (dim/8)^3 sub-cubes of 512 uint32 words each, sub-cubes x
+ *     fastest then y then z, voxels x fastest inside a sub-cube; a word is
+ *     (uint16 weight << 16) | uint16(int16 q) with TSDF = q / 32767.  A new
+ *     volume is every word 0x00007FFF (TSDF 1, weight 0).
+ *   dim, origin: 3 ints / 3 floats; K: host fx, fy, cx, cy; depth ww x hh
+ *   float metres and the 4x4 poses on the device, as vs_integrate_depth. */
+int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, const float* origin,
+                               float voxel_size, float mu, float max_w, const float* map_depth_dev,
+                               int ww, int hh, const float* K, const float* T_gc_dev,
+                               const float* T_cg_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -240,6 +240,11 @@ std::once_flag g_once;
 
 }  // namespace
 
+namespace vs {
+// lets other translation units report through vs_last_error()
+void set_error(const char* msg) { g_err = msg; }
+}  // namespace vs
+
 extern "C" {
 
 void vs_config_default(vs_config* c, int width, int height) {

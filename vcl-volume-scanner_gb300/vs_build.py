@@ -19,7 +19,7 @@ BUILD = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "vs_api.cu"]
+CU_SOURCES = ["k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "vs_api.cu", "vs_noalloc.cu"]
 HEADERS = ["vs_internal.cuh"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",

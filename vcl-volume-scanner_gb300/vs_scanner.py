@@ -113,6 +113,8 @@ _SIGS = {
     "vs_kernels_per_frame": (_I, [ctypes.POINTER(VsConfig)]),
     "vs_get_input_raw": (_I, [_P, _P]),
     "vs_get_device_buffer": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "vs_integrate_depth_noalloc": (_I, [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _I, _I, _P,
+                                        _P, _P, _P]),
 }
 
 _lib = None
