@@ -104,8 +104,8 @@ __global__ void k_pyramid_down(const float* __restrict__ in, int w, int h, float
 //   neighbours.  With C = code2 & ~R(row above), a row solves
 //   R_j = C_j & ~R_{j-1}: inside each run of C the rejected pixels alternate
 //   starting at the run's first pixel.  Runs are smeared with one addition
-//   per 32-bit word and the carry between words is a warp scan of
-//   {0,1} -> {0,1} maps.
+//   per 32-bit word; the words of a row and the rows themselves are swept as
+//   a wavefront across the lanes of the warp.
 // pass 3 (parallel): vertex valid = depth > 0 and not rejected; normal valid =
 //   code 1 and neither the left nor the upper neighbour rejected.
 // ---------------------------------------------------------------------------
@@ -114,6 +114,7 @@ struct LevelPtrs {
   float4* vtx;
   float4* nrm;
   uint8_t* code;
+  uint32_t* amask;
   uint32_t* rmask;
   int w, h;
   float K[4];
@@ -121,7 +122,8 @@ struct LevelPtrs {
 struct InmapArgs {
   LevelPtrs lv[kMaxLevels];
   int levels;
-  int tiles[kMaxLevels + 1];  // prefix of 16x16 tiles per level
+  int tiles[kMaxLevels + 1];  // prefix of tiles per level (32x8 for pre, 16x16 for post)
+  int tiles_pre[kMaxLevels + 1];
 };
 
 __device__ inline bool bp_valid(const float* depth, int w, int x, int y, const float* K, F3& p) {
@@ -131,14 +133,14 @@ __device__ inline bool bp_valid(const float* depth, int w, int x, int y, const f
   return true;
 }
 
-__global__ void k_inmap_pre(InmapArgs a) {
+__global__ void __launch_bounds__(256) k_inmap_pre(InmapArgs a) {
   int b = blockIdx.x, l = 0;
-  while (l + 1 < a.levels && b >= a.tiles[l + 1]) l++;
+  while (l + 1 < a.levels && b >= a.tiles_pre[l + 1]) l++;
   const LevelPtrs& L = a.lv[l];
-  int t = b - a.tiles[l];
-  int tw = (L.w + 15) / 16;
-  int x = (t % tw) * 16 + threadIdx.x, y = (t / tw) * 16 + threadIdx.y;
-  if (x >= L.w || y >= L.h) return;
+  const int t = b - a.tiles_pre[l];
+  const int tw = (L.w + 31) / 32;
+  const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * 8 + threadIdx.y;
+  if (y >= L.h) return;  // whole warp (a warp is one 32-pixel row segment)
   uint8_t code = 0;
   float4 n = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
   if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1) {
@@ -164,74 +166,61 @@ __global__ void k_inmap_pre(InmapArgs a) {
       }
     }
   }
+  const unsigned m = __ballot_sync(0xffffffffu, code == 2);
+  if (threadIdx.x == 0) L.amask[(size_t)y * tw + (t % tw)] = m;
+  if (x >= L.w) return;
   L.code[(size_t)y * L.w + x] = code;
   L.nrm[(size_t)y * L.w + x] = n;
 }
 
-// one block per level; warp 0 runs the row recurrence, the block first packs
-// the code-2 bits of the level into shared memory
+// one block per level: the block stages the level's code-2 bitmasks in
+// shared memory, then warp 0 sweeps the rows as a wavefront: at step t lane l
+// solves row t - l for its words, taking the carry of the row's earlier words
+// from lane l - 1 (computed at step t - 1) and the rejections of the row above
+// from its own registers, so one step costs one shuffle.
 __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
   extern __shared__ uint32_t amask[];  // [h][nw]
   const LevelPtrs& L = a.lv[blockIdx.x];
   const int nw = (L.w + 31) >> 5;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  for (int r = warp; r < L.h * nw; r += nwarps) {
-    int row = r / nw, word = r - row * nw;
-    int x = word * 32 + lane;
-    bool bit = false;
-    if (x < L.w) bit = L.code[(size_t)row * L.w + x] == 2;
-    uint32_t m = __ballot_sync(0xffffffffu, bit);
-    if (lane == 0) amask[r] = m;
-  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nwords = L.h * nw;
+  for (int i = threadIdx.x; i < nwords; i += blockDim.x) amask[i] = L.amask[i];
   __syncthreads();
   if (warp != 0) return;
   const uint32_t M0 = 0x55555555u, M1 = 0xaaaaaaaau;
-  // row 0 is never processed (interior rows only): no rejections
-  for (int c0 = 0; c0 < nw; c0 += 32) {
-    int w = c0 + lane;
-    if (w < nw) L.rmask[w] = 0u;
-  }
-  for (int row = 1; row < L.h; row++) {
-    uint32_t chunk_carry = 0;
-    for (int c0 = 0; c0 < nw; c0 += 32) {
-      int w = c0 + lane;
-      bool act = w < nw;
-      uint32_t A = act ? amask[row * nw + w] : 0u;
-      uint32_t Rup = act ? L.rmask[(size_t)(row - 1) * nw + w] : 0u;
-      uint32_t C = A & ~Rup;
-      uint32_t st = C & ~(C << 1);  // run starts (bit 0 counted as a start)
-      uint32_t rest = st & ~1u;
-      // word result for carry-in 0 and 1
-      uint32_t se0 = (rest & M0) | (st & 1u), so0 = rest & M1;
-      uint32_t se1 = rest & M0, so1 = (rest & M1) | (st & 1u);
-      uint32_t R0 = ((C & ((C + se0) ^ C)) & M0) | ((C & ((C + so0) ^ C)) & M1);
-      uint32_t R1 = ((C & ((C + se1) ^ C)) & M0) | ((C & ((C + so1) ^ C)) & M1);
-      // a run starting at bit 0 only continues the previous word's run when C bit 0 is set;
-      // if C bit 0 is clear the two results agree
-      uint32_t f0 = R0 >> 31, f1 = R1 >> 31;
-      // inclusive scan of the maps (f0, f1) over lanes
-      uint32_t g0 = f0, g1 = f1;
+  const int wpl = (nw + 31) >> 5;  // words per lane (1 up to 1024 pixels, 2 up to 2048)
+  uint32_t rup[2] = {0u, 0u};      // this lane's words of the row above
+  uint32_t cout_prev = 0u;
+  const int steps = L.h + 31;
+  for (int t = 0; t < steps; t++) {
+    uint32_t cin = __shfl_up_sync(0xffffffffu, cout_prev, 1);
+    if (lane == 0) cin = 0u;
+    const int row = t - lane;
+    uint32_t cout = 0u;
+    if (row >= 0 && row < L.h) {
 #pragma unroll
-      for (int d = 1; d < 32; d <<= 1) {
-        uint32_t b0 = __shfl_up_sync(0xffffffffu, g0, d);
-        uint32_t b1 = __shfl_up_sync(0xffffffffu, g1, d);
-        if (lane >= d) {
-          uint32_t n0 = b0 ? g1 : g0;
-          uint32_t n1 = b1 ? g1 : g0;
-          g0 = n0;
-          g1 = n1;
+      for (int q = 0; q < 2; q++) {
+        const int wi = lane * wpl + q;
+        if (q < wpl && wi < nw) {
+          uint32_t R = 0u;
+          if (row > 0) {  // row 0 is never processed (interior rows only)
+            const uint32_t C = amask[row * nw + wi] & ~rup[q];
+            const uint32_t st = C & ~(C << 1);  // run starts (bit 0 counted as a start)
+            const uint32_t rest = st & ~1u;
+            // runs starting at even / odd bits; a run at bit 0 continues the
+            // previous word's alternation, so its parity is the carry
+            const uint32_t se = (rest & M0) | (cin ? 0u : (st & 1u));
+            const uint32_t so = (rest & M1) | (cin ? (st & 1u) : 0u);
+            R = ((C & ((C + se) ^ C)) & M0) | ((C & ((C + so) ^ C)) & M1);
+          }
+          L.rmask[(size_t)row * nw + wi] = R;
+          rup[q] = R;
+          cin = R >> 31;
         }
       }
-      // carry into this lane = (prefix of lanes < lane)(chunk_carry)
-      uint32_t p0 = __shfl_up_sync(0xffffffffu, g0, 1);
-      uint32_t p1 = __shfl_up_sync(0xffffffffu, g1, 1);
-      uint32_t cin = (lane == 0) ? chunk_carry : (chunk_carry ? p1 : p0);
-      uint32_t R = cin ? R1 : R0;
-      if (act) L.rmask[(size_t)row * nw + w] = R;
-      uint32_t last = __shfl_sync(0xffffffffu, chunk_carry ? g1 : g0, 31);
-      chunk_carry = last;
+      cout = cin;
     }
-    __syncwarp();
+    cout_prev = cout;
   }
 }
 
@@ -270,18 +259,22 @@ InmapArgs make_inmap_args(const SessionDev& h) {
   InmapArgs a;
   a.levels = h.levels;
   a.tiles[0] = 0;
+  a.tiles_pre[0] = 0;
   for (int l = 0; l < kMaxLevels; l++) {
     LevelPtrs& L = a.lv[l];
     L.depth = h.depth[l];
     L.vtx = h.in_vtx[l];
     L.nrm = h.in_nrm[l];
     L.code = h.in_code[l];
+    L.amask = h.in_amask[l];
     L.rmask = h.in_rmask[l];
     L.w = h.lv[l].W;
     L.h = h.lv[l].H;
     for (int k = 0; k < 4; k++) L.K[k] = h.lv[l].K[k];
     int nt = (l < h.levels) ? ((L.w + 15) / 16) * ((L.h + 15) / 16) : 0;
     a.tiles[l + 1] = a.tiles[l] + nt;
+    int np = (l < h.levels) ? ((L.w + 31) / 32) * ((L.h + 7) / 8) : 0;
+    a.tiles_pre[l + 1] = a.tiles_pre[l] + np;
   }
   return a;
 }
@@ -320,7 +313,7 @@ size_t inmap_scan_smem(const SessionDev& h) {
 void launch_input_maps(const SessionDev* /*d*/, const SessionDev& h, cudaStream_t st) {
   InmapArgs a = make_inmap_args(h);
   dim3 b16(16, 16);
-  k_inmap_pre<<<a.tiles[h.levels], b16, 0, st>>>(a);
+  k_inmap_pre<<<a.tiles_pre[h.levels], dim3(32, 8), 0, st>>>(a);
   size_t smem = inmap_scan_smem(h);
   k_inmap_scan<<<h.levels, 1024, smem, st>>>(a);
   k_inmap_post<<<a.tiles[h.levels], b16, 0, st>>>(a);

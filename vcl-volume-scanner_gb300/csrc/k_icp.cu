@@ -101,6 +101,10 @@ __device__ inline void two_sum(float a, float b, float& s, float& e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
+// Per-thread sums of the (few) pixels a thread owns are plain float (FP32
+// and compensated modes) or double (FP64 mode); the compensated mode carries
+// (sum, error) pairs only from the warp shuffle tree on, where thousands of
+// values meet, so the pixel loop keeps 29 accumulators in registers.
 template <int MODE>
 struct Acc;
 template <>
@@ -111,6 +115,7 @@ struct Acc<VS_REDUCE_FP32> {
     for (int k = 0; k < 29; k++) s[k] = 0.0f;
   }
   __device__ void add(int k, float v) { s[k] += v; }
+  __device__ void begin_tree() {}
   __device__ void shfl_add(unsigned m) {
 #pragma unroll
     for (int k = 0; k < 29; k++) s[k] += __shfl_xor_sync(0xffffffffu, s[k], m);
@@ -122,13 +127,12 @@ struct Acc<VS_REDUCE_KAHAN> {
   float s[29], c[29];
   __device__ void zero() {
 #pragma unroll
-    for (int k = 0; k < 29; k++) s[k] = c[k] = 0.0f;
+    for (int k = 0; k < 29; k++) s[k] = 0.0f;
   }
-  __device__ void add(int k, float v) {
-    float t, e;
-    two_sum(s[k], v, t, e);
-    s[k] = t;
-    c[k] += e;
+  __device__ void add(int k, float v) { s[k] += v; }
+  __device__ void begin_tree() {
+#pragma unroll
+    for (int k = 0; k < 29; k++) c[k] = 0.0f;
   }
   __device__ void shfl_add(unsigned m) {
 #pragma unroll
@@ -151,6 +155,7 @@ struct Acc<VS_REDUCE_FP64> {
     for (int k = 0; k < 29; k++) s[k] = 0.0;
   }
   __device__ void add(int k, float v) { s[k] += (double)v; }
+  __device__ void begin_tree() {}
   __device__ void shfl_add(unsigned m) {
 #pragma unroll
     for (int k = 0; k < 29; k++) s[k] += __shfl_xor_sync(0xffffffffu, s[k], m);
@@ -172,121 +177,161 @@ __device__ inline double2 combine(double2 a, double2 b) {
 
 __device__ inline int tri_index(int i, int j) { return i * 6 - i * (i - 1) / 2 + (j - i); }
 
-// ---- FP64 pose algebra (single thread) ------------------------------------
-__device__ void mat4_mul(const double* a, const double* b, double* c) {
-  for (int j = 0; j < 4; j++)
-    for (int i = 0; i < 4; i++) {
-      double s = 0.0;
-      for (int k = 0; k < 4; k++) s += a[j * 4 + k] * b[k * 4 + i];
-      c[j * 4 + i] = s;
-    }
+// ---- FP64 pose algebra, spread over the lanes of one warp ------------------
+// FP64 runs on a narrow pipe on this part: a dependent double operation costs
+// tens of cycles whatever the number of active lanes, so the 6x6 solve, the
+// SE(3) exponential and the 4x4 products keep every lane busy on its own
+// matrix element instead of running as one long single-thread chain.
+
+// lane -> (row, col) of the lower triangle, row-major: lane = row*(row+1)/2 + col
+__device__ __forceinline__ int low_lane(int r, int c) { return r * (r + 1) / 2 + c; }
+__device__ __forceinline__ void low_rc(int lane, int& r, int& c) {
+  r = 0;
+  while (low_lane(r + 1, 0) <= lane) r++;
+  c = lane - low_lane(r, 0);
 }
-// inverse of a rigid transform [R t; 0 1]
+
+// d_lld_LL_Decomposition + d_sls_Solve_Linear_System_using_LLD as L D L^T in
+// FP64 (D_j = L_jj^2) with the reference's outcomes: a pivot with
+// sqrt(D_j) < 1e-8 fails the solve (returns 1); a negative (or NaN) pivot
+// makes the reference's square root NaN, its column zero and the solution
+// NaN, which the convergence test then reads as converged (returns 2);
+// otherwise returns 0 and lane i < 6 holds x_i.
+__device__ int warp_solve6(const double* fin, int lane, double& x) {
+  const unsigned M = 0xffffffffu;
+  int r = 0, c = 0;
+  if (lane < 21) low_rc(lane, r, c);
+  double a = (lane < 21) ? fin[tri_index(c, r)] : 0.0;
+  bool nanp = false, fail = false;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const double d = __shfl_sync(M, a, low_lane(j, j));
+    const bool neg = !(d >= 0.0);
+    const bool tiny = !neg && d < 1e-16;
+    nanp |= neg;
+    fail |= tiny;
+    const bool ok = !neg && !tiny;
+    const double rd = 1.0 / d;
+    if (lane < 21 && c == j && r > j) a = ok ? a * rd : 0.0;
+    const bool upd = lane < 21 && c > j;
+    const double lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
+    const double lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
+    if (upd && ok) a -= lr * d * lc;
+  }
+  if (fail) return 1;
+  // L y = b, z = y / D, L^T x = z
+  double y = (lane < 6) ? fin[21 + lane] : 0.0;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const double yj = __shfl_sync(M, y, j);
+    const bool upd = lane < 6 && lane > j;
+    const double l = __shfl_sync(M, a, upd ? low_lane(lane, j) : lane);
+    if (upd) y -= l * yj;
+  }
+  const double D = __shfl_sync(M, a, lane < 6 ? low_lane(lane, lane) : lane);
+  double z = (lane < 6) ? y / D : 0.0;
+#pragma unroll
+  for (int j = 5; j >= 0; j--) {
+    const double xj = __shfl_sync(M, z, j);
+    const bool upd = lane < j;
+    const double l = __shfl_sync(M, a, upd ? low_lane(j, lane) : lane);
+    if (upd) z -= l * xj;
+  }
+  x = z;
+  return nanp ? 2 : 0;
+}
+
+// SE(3) exponential in the reference's parameterisation
+// (z_uitme_Update_Incremental_Tracking_with_Matrix_Exponential,
+// z_yooji_cuda_pose_tracker.cu:50-149): with th = |w| and u = w / th,
+// R = I + sin(th)[u]x + (1 - cos(th))[u]x^2 and
+// t = (I - R)[u]x v / th + u u^T v; [u]x^2 = u u^T - I.  For th < 0.1 sin and
+// 1 - cos come from their Taylor series (through th^11 and th^12, truncation
+// below 1e-20 relative); below th = 1e-10 the first-order limit R = I + [w]x,
+// t = v is used (the reference divides by th unguarded).  Lane l < 16 returns
+// element l of the 4x4 result; x is lane i's twist component.
+__device__ double warp_se3_exp(double x, int lane) {
+  const unsigned M = 0xffffffffu;
+  double q[6];
+#pragma unroll
+  for (int k = 0; k < 6; k++) q[k] = __shfl_sync(M, x, k);
+  const int r = (lane >> 2) & 3, cc = lane & 3;
+  if (lane >= 16 || r == 3) return (lane == 15) ? 1.0 : 0.0;
+  const double th2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+  const double th = sqrt(th2);
+  if (th < 1e-10) {
+    const double wx[9] = {0.0, -q[2], q[1], q[2], 0.0, -q[0], -q[1], q[0], 0.0};
+    if (cc == 3) return q[3 + r];
+    return (r == cc ? 1.0 : 0.0) + wx[r * 3 + cc];
+  }
+  double sn, cs;
+  if (th < 0.1) {
+    sn = th * (1.0 - th2 / 6.0 * (1.0 - th2 / 20.0 * (1.0 - th2 / 42.0 * (1.0 - th2 / 72.0 * (1.0 - th2 / 110.0)))));
+    cs = th2 / 2.0 *
+         (1.0 - th2 / 12.0 * (1.0 - th2 / 30.0 * (1.0 - th2 / 56.0 * (1.0 - th2 / 90.0 * (1.0 - th2 / 132.0)))));
+  } else {
+    sn = sin(th);
+    cs = 1.0 - cos(th);
+  }
+  const double it = 1.0 / th;
+  const double u[3] = {q[0] * it, q[1] * it, q[2] * it};
+  const double v[3] = {q[3] * it, q[4] * it, q[5] * it};
+  const double ux[9] = {0.0, -u[2], u[1], u[2], 0.0, -u[0], -u[1], u[0], 0.0};
+  double R[3];  // row r of R
+#pragma unroll
+  for (int k = 0; k < 3; k++) R[k] = (r == k ? 1.0 : 0.0) + sn * ux[r * 3 + k] + cs * (u[r] * u[k] - (r == k ? 1.0 : 0.0));
+  if (cc < 3) return R[cc];
+  const double uv[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
+  const double udv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+  double t = u[r] * udv * th;
+#pragma unroll
+  for (int k = 0; k < 3; k++) t += ((r == k ? 1.0 : 0.0) - R[k]) * uv[k];
+  return t;
+}
+
+// out = A * B (4x4, lane l < 16 computes element l); A in shared memory
+__device__ void warp_compose(const double* A, const double* B, double* out, int lane) {
+  if (lane < 16) {
+    const int r = lane >> 2, c = lane & 3;
+    double s = 0.0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) s += A[r * 4 + k] * B[k * 4 + c];
+    out[lane] = s;
+  }
+  __syncwarp();
+}
+// inverse of a rigid transform [R t; 0 1] held in shared memory; lane l < 16
+// receives element l
+__device__ void warp_rigid_inverse(const double* T, int lane, double& out) {
+  out = 0.0;
+  if (lane < 16) {
+    const int r = lane >> 2, c = lane & 3;
+    if (r == 3)
+      out = (c == 3) ? 1.0 : 0.0;
+    else if (c < 3)
+      out = T[c * 4 + r];
+    else
+      out = -(T[0 * 4 + r] * T[3] + T[1 * 4 + r] * T[7] + T[2 * 4 + r] * T[11]);
+  }
+}
+// T12 <- E * T12 and T21 = float(inv(T12)); E and scratch Tn in shared memory
+__device__ void warp_compose_and_invert(const double* E, double* T12, double* Tn, int lane, double* T12_out,
+                                        float* T21_out) {
+  warp_compose(E, T12, Tn, lane);
+  double ti;
+  warp_rigid_inverse(Tn, lane, ti);
+  if (lane < 16) {
+    T12_out[lane] = Tn[lane];
+    T21_out[lane] = (float)ti;
+  }
+}
+// single-thread inverse used once per frame by k_icp_begin
 __device__ void rigid_inverse(const double* T, double* I) {
   for (int i = 0; i < 3; i++)
     for (int j = 0; j < 3; j++) I[i * 4 + j] = T[j * 4 + i];
   for (int i = 0; i < 3; i++) I[i * 4 + 3] = -(T[0 * 4 + i] * T[3] + T[1 * 4 + i] * T[7] + T[2 * 4 + i] * T[11]);
   I[12] = I[13] = I[14] = 0.0;
   I[15] = 1.0;
-}
-// SE(3) exponential in the reference's parameterisation
-// (z_uitme_Update_Incremental_Tracking_with_Matrix_Exponential, :50-149):
-// R = I + sin(th)[w]x + (1-cos(th))[w]x^2 with w normalised,
-// t = (I-R)[w]x v/th + w w^T v; below th = 1e-10 the first-order limit is used
-// (the reference divides by th unguarded).
-__device__ void se3_exp(const double* xi, double* E) {
-  double th = sqrt(xi[0] * xi[0] + xi[1] * xi[1] + xi[2] * xi[2]);
-  for (int i = 0; i < 16; i++) E[i] = 0.0;
-  E[15] = 1.0;
-  if (th < 1e-10) {
-    E[0] = E[5] = E[10] = 1.0;
-    E[1] = -xi[2];
-    E[2] = xi[1];
-    E[4] = xi[2];
-    E[6] = -xi[0];
-    E[8] = -xi[1];
-    E[9] = xi[0];
-    E[3] = xi[3];
-    E[7] = xi[4];
-    E[11] = xi[5];
-    return;
-  }
-  double w[3] = {xi[0] / th, xi[1] / th, xi[2] / th};
-  double v[3] = {xi[3] / th, xi[4] / th, xi[5] / th};
-  double wx[9] = {0.0, -w[2], w[1], w[2], 0.0, -w[0], -w[1], w[0], 0.0};
-  double wx2[9];
-  for (int j = 0; j < 3; j++)
-    for (int i = 0; i < 3; i++) {
-      double s = 0.0;
-      for (int k = 0; k < 3; k++) s += wx[j * 3 + k] * wx[k * 3 + i];
-      wx2[j * 3 + i] = s;
-    }
-  double sn = sin(th), cs = 1.0 - cos(th);
-  double R[9], M[9];
-  for (int i = 0; i < 9; i++) R[i] = sn * wx[i] + cs * wx2[i];
-  for (int i = 0; i < 9; i++) M[i] = -R[i];  // I - R without the identity
-  R[0] += 1.0;
-  R[4] += 1.0;
-  R[8] += 1.0;
-  double wv = w[0] * v[0] + w[1] * v[1] + w[2] * v[2];
-  for (int j = 0; j < 3; j++) {
-    double s = 0.0;
-    for (int i = 0; i < 3; i++) {
-      double mw = 0.0;
-      for (int k = 0; k < 3; k++) mw += M[j * 3 + k] * wx[k * 3 + i];
-      s += mw * v[i];
-    }
-    E[j * 4 + 3] = s + w[j] * wv * th;
-  }
-  for (int j = 0; j < 3; j++)
-    for (int i = 0; i < 3; i++) E[j * 4 + i] = R[j * 3 + i];
-}
-
-// d_lld_LL_Decomposition + d_sls_Solve_Linear_System_using_LLD in FP64 with
-// the reference's rules: a pivot whose magnitude is below 1e-8 fails the
-// solve; a negative pivot (square root of a negative number) propagates NaN,
-// which the infinity-norm test then treats as converged.
-__device__ bool solve6(const double* A, const double* b, double* x) {
-  double L[36];
-  for (int i = 0; i < 36; i++) L[i] = 0.0;
-  for (int i = 0; i < 6; i++)
-    for (int j = 0; j <= i; j++) {
-      if (i == j) {
-        double s = 0.0;
-        for (int k = 0; k < j; k++) s += L[j * 6 + k] * L[j * 6 + k];
-        L[j * 6 + j] = sqrt(A[j * 6 + j] - s);
-      } else if (fabs(L[j * 6 + j]) >= 1e-8) {
-        double s = 0.0;
-        for (int k = 0; k < j; k++) s += L[i * 6 + k] * L[j * 6 + k];
-        L[i * 6 + j] = (A[i * 6 + j] - s) / L[j * 6 + j];
-      }
-    }
-  for (int i = 0; i < 6; i++)
-    if (fabs(L[i * 6 + i]) < 1e-8) return false;
-  double y[6];
-  for (int i = 0; i < 6; i++) {
-    double s = 0.0;
-    for (int k = 0; k < i; k++) s += L[i * 6 + k] * y[k];
-    y[i] = (b[i] - s) / L[i * 6 + i];
-  }
-  for (int i = 5; i >= 0; i--) {
-    double s = 0.0;
-    for (int k = i + 1; k < 6; k++) s += L[k * 6 + i] * x[k];
-    x[i] = (y[i] - s) / L[i * 6 + i];
-  }
-  return true;
-}
-
-__device__ void refresh_float_pose(Pose* P) {
-  double I[16];
-  rigid_inverse(P->T_gc, I);
-  for (int i = 0; i < 16; i++) {
-    P->Tgc[i] = (float)P->T_gc[i];
-    P->Tcg[i] = (float)I[i];
-  }
-  P->center[0] = (float)I[3];
-  P->center[1] = (float)I[7];
-  P->center[2] = (float)I[11];
 }
 
 __global__ void k_icp_begin(SessionDev* s, int allow_skip, int with_init, const float* init) {
@@ -309,7 +354,7 @@ __global__ void k_icp_begin(SessionDev* s, int allow_skip, int with_init, const 
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(kThreads) k_icp_iter(const SessionDev* __restrict__ s, int level) {
+__global__ void __launch_bounds__(kThreads, 3) k_icp_iter(const SessionDev* __restrict__ s, int level) {
   Pose* P = s->pose;
   if (P->skip | P->failed | P->level_done[level]) return;  // uniform across the grid
   const int w = s->lv[level].W, h = s->lv[level].H;
@@ -340,6 +385,7 @@ __global__ void __launch_bounds__(kThreads) k_icp_iter(const SessionDev* __restr
     acc.add(27, 1.0f);
     acc.add(28, b * b);
   }
+  acc.begin_tree();
 #pragma unroll
   for (int m = 16; m >= 1; m >>= 1) acc.shfl_add(m);
 
@@ -387,62 +433,73 @@ __global__ void __launch_bounds__(kThreads) k_icp_iter(const SessionDev* __restr
     if (k < 29 && j == 0) fin[k] = v.x + v.y;
   }
   __syncthreads();
-  if (threadIdx.x != 0) return;
-  *s->icp_counter = 0u;
-  double A6[36], b6[6], x[6];
-  for (int i = 0; i < 6; i++)
-    for (int j = i; j < 6; j++) A6[i * 6 + j] = A6[j * 6 + i] = fin[tri_index(i, j)];
-  for (int i = 0; i < 6; i++) b6[i] = fin[21 + i];
-  for (int k = 0; k < 29; k++) P->last_sums[k] = fin[k];
-  P->iters_run += 1;
-  P->valid_count = (int)fin[27];
-  if (!solve6(A6, b6, x)) {
-    P->failed = 1;
+  if (threadIdx.x >= 32) return;
+  // ---- warp 0: FP64 solve and SE(3) update, lane-parallel ----
+  const int ln = threadIdx.x;
+  if (ln == 0) *s->icp_counter = 0u;
+  if (ln < 29) P->last_sums[ln] = fin[ln];
+  if (ln == 0) {
+    P->iters_run += 1;
+    P->valid_count = (int)fin[27];
+  }
+  double x;
+  const int st = warp_solve6(fin, ln, x);
+  if (st == 1) {
+    if (ln == 0) P->failed = 1;
     return;
   }
-  for (int i = 0; i < 6; i++) P->last_x[i] = (float)x[i];
-  // d_niv_Norm_Infinity_Vector: NaN entries never raise the maximum
-  double ninf = -100000.0;
-  for (int i = 0; i < 6; i++) {
-    double a = fabs(x[i]);
-    if (ninf < a) ninf = a;
-  }
-  if (ninf < 5.0e-7) {
-    P->level_done[level] = 1;
+  if (ln < 6) P->last_x[ln] = (float)x;
+  // |x|_inf < 5e-7 ends the level (d_niv_Norm_Infinity_Vector: NaN entries never
+  // raise the maximum, so an all-NaN solution also ends it)
+  const bool big = (ln < 6) && (fabs(x) >= 5.0e-7);
+  if (st == 2 || !__any_sync(0xffffffffu, big)) {
+    if (ln == 0) P->level_done[level] = 1;
     return;
   }
-  double E[16], T[16], I[16];
-  se3_exp(x, E);
-  mat4_mul(E, P->T12, T);
-  rigid_inverse(T, I);
-  for (int i = 0; i < 16; i++) {
-    P->T12[i] = T[i];
-    P->T21[i] = (float)I[i];
-  }
+  __shared__ double E[16], Tn[16];
+  const double e = warp_se3_exp(x, ln);
+  if (ln < 16) E[ln] = e;
+  __syncwarp();
+  warp_compose_and_invert(E, P->T12, Tn, ln, P->T12, P->T21);
 }
 
 __global__ void k_icp_finish(SessionDev* s, int frame_mode) {
   Pose* P = s->pose;
-  if (!P->skip) {
-    if (!P->failed) {
-      double T[16];
-      mat4_mul(P->T12, P->T_gc, T);
-      for (int i = 0; i < 16; i++) P->T_gc[i] = T[i];
-      refresh_float_pose(P);
-      P->tracked = 1;
-    } else {
-      P->tracked = 0;
+  const int ln = threadIdx.x;
+  __shared__ double Tn[16], A[16];
+  if (!P->skip && !P->failed) {
+    if (ln < 16) A[ln] = P->T12[ln];
+    __syncwarp();
+    double Ti;
+    warp_compose(A, P->T_gc, Tn, ln);
+    if (ln < 16) P->T_gc[ln] = Tn[ln];
+    warp_rigid_inverse(Tn, ln, Ti);
+    if (ln < 16) {
+      P->Tgc[ln] = (float)Tn[ln];
+      P->Tcg[ln] = (float)Ti;
     }
-  } else {
-    P->tracked = 1;
+    if (ln == 3 || ln == 7 || ln == 11) P->center[ln >> 2] = (float)Ti;
   }
-  if (frame_mode) P->frame += 1;
+  if (ln == 0) {
+    P->tracked = P->skip ? 1 : (P->failed ? 0 : 1);
+    if (frame_mode) P->frame += 1;
+  }
 }
 
 __global__ void k_pose_set(SessionDev* s, const double* T) {
   Pose* P = s->pose;
-  for (int i = 0; i < 16; i++) P->T_gc[i] = T[i];
-  refresh_float_pose(P);
+  const int ln = threadIdx.x;
+  __shared__ double Tn[16];
+  if (ln < 16) Tn[ln] = T[ln];
+  __syncwarp();
+  double Ti;
+  warp_rigid_inverse(Tn, ln, Ti);
+  if (ln < 16) {
+    P->T_gc[ln] = Tn[ln];
+    P->Tgc[ln] = (float)Tn[ln];
+    P->Tcg[ln] = (float)Ti;
+  }
+  if (ln == 3 || ln == 7 || ln == 11) P->center[ln >> 2] = (float)Ti;
 }
 
 int icp_blocks(int npix) {
@@ -478,11 +535,11 @@ void launch_icp(const SessionDev* d, const SessionDev& h, cudaStream_t st, bool 
       }
     }
   }
-  k_icp_finish<<<1, 1, 0, st>>>(dm, frame_mode ? 1 : 0);
+  k_icp_finish<<<1, 32, 0, st>>>(dm, frame_mode ? 1 : 0);
 }
 
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st) {
-  k_pose_set<<<1, 1, 0, st>>>(const_cast<SessionDev*>(d), T_gc);
+  k_pose_set<<<1, 32, 0, st>>>(const_cast<SessionDev*>(d), T_gc);
 }
 
 }  // namespace vs

@@ -153,7 +153,11 @@ __global__ void __launch_bounds__(kIntThreads)
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
     if (lane == 0) {
       s->brick_flag[b] = 0u;
-      if (nupd) atomicAdd(s->brick_count + 1, (uint32_t)nupd);
+      if (nupd) {
+        atomicAdd(s->brick_count + 1, (uint32_t)nupd);
+        // weights never decrease, so a brick that got an update stays occupied
+        if (s->occ) atomicOr(s->occ + (b >> 5), 1u << (b & 31));
+      }
     }
   }
 }
@@ -195,6 +199,26 @@ __global__ void k_volume_import(typename S::word* vol, int X, int Y, int z0, int
     if (tsdf) t = tsdf[i];
     if (w) ww = w[i];
     vol[idx] = S::encode(t, ww);
+  }
+}
+
+// recomputes the occupancy bits from the weights (after a volume import);
+// one warp per brick
+template <class S>
+__global__ void k_occupancy(const typename S::word* vol, size_t nbr, uint32_t* occ) {
+  const int lane = threadIdx.x & 31;
+  const size_t gw = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarp = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t b = gw; b < nbr; b += nwarp) {
+    bool any = false;
+    for (int k = lane; k < kBrickVox; k += 32) {
+      float t;
+      uint32_t w;
+      S::decode(vol[b * kBrickVox + k], t, w);
+      any |= w != 0u;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, any);
+    if (lane == 0 && m) atomicOr(occ + (b >> 5), 1u << (b & 31));
   }
 }
 
@@ -273,6 +297,23 @@ void launch_volume_slab(const SessionDev& h, bool do_export, int z0, int nz, flo
                                                           h.nb[1], tsdf, w);
       else
         k_volume_import<StoreI16><<<blocks, 256, 0, st>>>((uint32_t*)h.vol, X, Y, z0, nz, h.nb[0], h.nb[1], tsdf, w);
+      break;
+  }
+}
+
+void launch_occupancy_rebuild(const SessionDev& h, cudaStream_t st) {
+  const size_t nbr = (size_t)h.nb[0] * h.nb[1] * h.nb[2];
+  cudaMemsetAsync(h.occ, 0, ((nbr + 31) / 32) * 4, st);
+  const int blocks = sm_count() * 8;
+  switch (h.tsdf_type) {
+    case VS_TSDF_FP16:
+      k_occupancy<StoreF16><<<blocks, 256, 0, st>>>((const uint32_t*)h.vol, nbr, h.occ);
+      break;
+    case VS_TSDF_FP32:
+      k_occupancy<StoreF32><<<blocks, 256, 0, st>>>((const uint2*)h.vol, nbr, h.occ);
+      break;
+    default:
+      k_occupancy<StoreI16><<<blocks, 256, 0, st>>>((const uint32_t*)h.vol, nbr, h.occ);
       break;
   }
 }

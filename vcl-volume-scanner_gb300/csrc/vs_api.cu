@@ -170,6 +170,7 @@ int reset_state(vs_session* s) {
   VS_CU(cudaMemsetAsync(s->h.brick_flag, 0, sizeof(uint32_t) * (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2],
                         s->stream));
   VS_CU(cudaMemsetAsync(s->h.brick_count, 0, sizeof(uint32_t), s->stream));
+  VS_CU(cudaMemsetAsync(s->h.occ, 0, (((size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2] + 31) / 32) * 4, s->stream));
   VS_CU(cudaMemsetAsync(s->h.icp_counter, 0, sizeof(unsigned), s->stream));
   Pose p;
   std::memset(&p, 0, sizeof(p));
@@ -284,12 +285,12 @@ size_t vs_session_bytes(const vs_config* c) {
   if (check_config(c) != VS_OK) return 0;
   size_t b = volume_bytes(c);
   size_t nbr = (size_t)(c->dim[0] / 8) * (c->dim[1] / 8) * (c->dim[2] / 8);
-  b += 2 * nbr * 4 + 64;
+  b += 2 * nbr * 4 + ((nbr + 31) / 32) * 4 + 64;
   int w = c->width, h = c->height;
   b += (size_t)w * h * (2 + 4 + 4);
   for (int l = 0; l < c->levels; l++) {
     size_t n = (size_t)(w >> l) * (h >> l);
-    b += n * (4 + 16 + 16 + 1 + 4 + 16 + 16 + 1) + (size_t)(h >> l) * (((w >> l) + 31) / 32) * 4;
+    b += n * (4 + 16 + 16 + 1 + 4 + 16 + 16 + 1) + 2 * (size_t)(h >> l) * (((w >> l) + 31) / 32) * 4;
   }
   b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + 64;
   return b;
@@ -328,6 +329,7 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.brick_flag, nbr * 4);
   rc |= alloc(s, &h.brick_list, nbr * 4);
   rc |= alloc(s, &h.brick_count, 64);
+  rc |= alloc(s, &h.occ, ((nbr + 31) / 32) * 4);
   rc |= alloc(s, &h.depth_mm, n0 * 2);
   rc |= alloc(s, &h.depth_raw, n0 * 4);
   rc |= alloc(s, &s->stage_f, n0 * 4);
@@ -338,6 +340,7 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
     rc |= alloc(s, &h.in_vtx[l], n * 16);
     rc |= alloc(s, &h.in_nrm[l], n * 16);
     rc |= alloc(s, &h.in_code[l], n);
+    rc |= alloc(s, &h.in_amask[l], (size_t)h.lv[l].H * ((h.lv[l].W + 31) / 32) * 4);
     rc |= alloc(s, &h.in_rmask[l], (size_t)h.lv[l].H * ((h.lv[l].W + 31) / 32) * 4);
     rc |= alloc(s, &h.m_depth[l], n * 4);
     rc |= alloc(s, &h.m_vtx[l], n * 16);
@@ -566,6 +569,10 @@ static int volume_transfer(vs_session* s, bool do_export, float* tsdf, uint16_t*
         launch_volume_slab(s->h, false, z0, nz, tsdf_in ? dt : nullptr, w_in ? dw : nullptr, s->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  }
+  if (e == cudaSuccess && !do_export) {
+    launch_occupancy_rebuild(s->h, s->stream);
+    e = cudaStreamSynchronize(s->stream);
   }
   cudaFree(dt);
   cudaFree(dw);

@@ -19,7 +19,7 @@ constexpr int kBrick = 8;             // 8^3 voxels per brick = reference sub-cu
 constexpr int kBrickVox = 512;
 constexpr float kQ = 32767.0f;
 constexpr int kPartials = 32;         // doubles per ICP block partial (29 used)
-constexpr int kIcpMaxBlocks = 304;    // 2 blocks per SM on 152 SMs
+constexpr int kIcpMaxBlocks = 456;    // 3 blocks per SM on 152 SMs
 
 struct Level {
   int W, H;
@@ -69,6 +69,7 @@ struct SessionDev {
   float4* in_vtx[kMaxLevels];    // input vertex map (w = 1 valid, 0 invalid)
   float4* in_nrm[kMaxLevels];    // input normal map (w = 1 valid)
   uint8_t* in_code[kMaxLevels];  // normal-map pre-pass codes
+  uint32_t* in_amask[kMaxLevels];// per-row bitmasks of normals failing the angle test
   uint32_t* in_rmask[kMaxLevels];// per-row rejection bitmasks
   float* m_depth[kMaxLevels];    // model (ray-cast) maps
   float4* m_vtx[kMaxLevels];     // xyz, w = 1 valid (invalid: -100)
@@ -79,6 +80,7 @@ struct SessionDev {
   uint32_t* brick_flag;          // per brick: 1 while listed this frame
   uint32_t* brick_list;          // active bricks of this frame
   uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame)
+  uint32_t* occ;                 // 1 bit per brick: some voxel has weight > 0 (NULL: not kept)
   // ICP scratch
   double* partials;              // [kIcpMaxBlocks][2*kPartials]
   unsigned* icp_counter;
@@ -211,6 +213,7 @@ void launch_volume_export(const SessionDev& h, float* tsdf, uint16_t* w, cudaStr
 void launch_volume_import(const SessionDev& h, const float* tsdf, const uint16_t* w,
                           cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
+void launch_occupancy_rebuild(const SessionDev& h, cudaStream_t st);
 void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3,
                         float* inrm3, cudaStream_t st);
 
