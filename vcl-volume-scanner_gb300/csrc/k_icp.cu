@@ -120,7 +120,7 @@ struct Acc<VS_REDUCE_FP32> {
 #pragma unroll
     for (int k = 0; k < 29; k++) s[k] += __shfl_xor_sync(0xffffffffu, s[k], m);
   }
-  __device__ double2 get(int k) const { return make_double2((double)s[k], 0.0); }
+  __device__ float2 get(int k) const { return make_float2(s[k], 0.0f); }
 };
 template <>
 struct Acc<VS_REDUCE_KAHAN> {
@@ -145,7 +145,7 @@ struct Acc<VS_REDUCE_KAHAN> {
       c[k] = c[k] + oc + e;
     }
   }
-  __device__ double2 get(int k) const { return make_double2((double)s[k], (double)c[k]); }
+  __device__ float2 get(int k) const { return make_float2(s[k], c[k]); }
 };
 template <>
 struct Acc<VS_REDUCE_FP64> {
@@ -163,16 +163,29 @@ struct Acc<VS_REDUCE_FP64> {
   __device__ double2 get(int k) const { return make_double2(s[k], 0.0); }
 };
 
-// combine two partials (hi, lo) in the mode's arithmetic
+// Partial sums travel as (sum, error) pairs in the mode's own type: float2
+// for the FP32 and compensated modes (no conversions to double, which run on
+// the narrow FP64 pipe), double2 for the FP64 mode.
 template <int MODE>
-__device__ inline double2 combine(double2 a, double2 b) {
-  if (MODE == VS_REDUCE_FP32) return make_double2((double)((float)a.x + (float)b.x), 0.0);
-  if (MODE == VS_REDUCE_KAHAN) {
-    float t, e;
-    two_sum((float)a.x, (float)b.x, t, e);
-    return make_double2((double)t, (double)((float)a.y + (float)b.y + e));
-  }
-  return make_double2(a.x + b.x, 0.0);
+struct PartT {
+  typedef float2 type;
+};
+template <>
+struct PartT<VS_REDUCE_FP64> {
+  typedef double2 type;
+};
+__device__ inline float2 combine(float2 a, float2 b, int mode) {
+  if (mode == VS_REDUCE_FP32) return make_float2(a.x + b.x, 0.0f);
+  float t, e;
+  two_sum(a.x, b.x, t, e);
+  return make_float2(t, a.y + b.y + e);
+}
+__device__ inline double2 combine(double2 a, double2 b, int) { return make_double2(a.x + b.x, 0.0); }
+__device__ inline float2 shfl_xor2(float2 v, int m) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
+}
+__device__ inline double2 shfl_xor2(double2 v, int m) {
+  return make_double2(__shfl_xor_sync(0xffffffffu, v.x, m), __shfl_xor_sync(0xffffffffu, v.y, m));
 }
 
 __device__ inline int tri_index(int i, int j) { return i * 6 - i * (i - 1) / 2 + (j - i); }
@@ -191,102 +204,125 @@ __device__ __forceinline__ void low_rc(int lane, int& r, int& c) {
   c = lane - low_lane(r, 0);
 }
 
-// d_lld_LL_Decomposition + d_sls_Solve_Linear_System_using_LLD as L D L^T in
-// FP64 (D_j = L_jj^2) with the reference's outcomes: a pivot with
-// sqrt(D_j) < 1e-8 fails the solve (returns 1); a negative (or NaN) pivot
-// makes the reference's square root NaN, its column zero and the solution
-// NaN, which the convergence test then reads as converged (returns 2);
-// otherwise returns 0 and lane i < 6 holds x_i.
+// The 6x6 solve: d_lld_LL_Decomposition + d_sls_Solve_Linear_System_using_LLD
+// (_yooji_cuda_math.h:489-592), restated as an L D L^T factorisation
+// (D_j = L_jj^2) in float - the reference's own precision, so its pivot rules
+// apply unchanged: a pivot with sqrt(D_j) < 1e-8 fails the solve (returns 1);
+// a negative or NaN pivot makes the reference's square root NaN, its column
+// zero and the solution NaN, which the convergence test reads as converged
+// (returns 2).  The solution is then refined twice against the FP64 normal
+// equations: r = b - A x in double, A d = r with the float factors,
+// x += d in double.  The refined x agrees with an FP64 solve to FP64 rounding
+// for condition numbers up to ~1e6 while the narrow FP64 pipe only carries
+// the residuals.  Lane i < 6 returns x_i.
+__device__ void warp_ldl_solve_f32(float l, float D, int lane, int r, int c, float& v) {
+  const unsigned M = 0xffffffffu;
+  // v: right-hand side in lanes 0..5 on entry, solution on exit
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const float vj = __shfl_sync(M, v, j);
+    const bool upd = lane < 6 && lane > j;
+    const float lij = __shfl_sync(M, l, upd ? low_lane(lane, j) : lane);
+    if (upd) v -= lij * vj;
+  }
+  const float dd = __shfl_sync(M, D, lane < 6 ? low_lane(lane, lane) : lane);
+  if (lane < 6) v = v / dd;
+#pragma unroll
+  for (int j = 5; j >= 0; j--) {
+    const float xj = __shfl_sync(M, v, j);
+    const bool upd = lane < j;
+    const float lji = __shfl_sync(M, l, upd ? low_lane(j, lane) : lane);
+    if (upd) v -= lji * xj;
+  }
+  (void)r;
+  (void)c;
+}
+
 __device__ int warp_solve6(const double* fin, int lane, double& x) {
   const unsigned M = 0xffffffffu;
   int r = 0, c = 0;
   if (lane < 21) low_rc(lane, r, c);
-  double a = (lane < 21) ? fin[tri_index(c, r)] : 0.0;
+  float a = (lane < 21) ? (float)fin[tri_index(c, r)] : 0.0f;
   bool nanp = false, fail = false;
 #pragma unroll
   for (int j = 0; j < 6; j++) {
-    const double d = __shfl_sync(M, a, low_lane(j, j));
-    const bool neg = !(d >= 0.0);
-    const bool tiny = !neg && d < 1e-16;
+    const float d = __shfl_sync(M, a, low_lane(j, j));
+    const bool neg = !(d >= 0.0f);
+    const bool tiny = !neg && !(sqrtf(d) >= 1e-8f);
     nanp |= neg;
     fail |= tiny;
     const bool ok = !neg && !tiny;
-    const double rd = 1.0 / d;
-    if (lane < 21 && c == j && r > j) a = ok ? a * rd : 0.0;
+    if (lane < 21 && c == j && r > j) a = ok ? a / d : 0.0f;
     const bool upd = lane < 21 && c > j;
-    const double lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
-    const double lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
+    const float lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
+    const float lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
     if (upd && ok) a -= lr * d * lc;
   }
   if (fail) return 1;
-  // L y = b, z = y / D, L^T x = z
-  double y = (lane < 6) ? fin[21 + lane] : 0.0;
+  // a now holds L (strict lower part) and D (diagonal lanes)
+  float v = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
+  warp_ldl_solve_f32(a, a, lane, r, c, v);
+  x = (lane < 6) ? (double)v : 0.0;
+  if (nanp) return 2;
+  // iterative refinement on the FP64 system
+  for (int it = 0; it < 2; it++) {
+    double xk[6];
 #pragma unroll
-  for (int j = 0; j < 6; j++) {
-    const double yj = __shfl_sync(M, y, j);
-    const bool upd = lane < 6 && lane > j;
-    const double l = __shfl_sync(M, a, upd ? low_lane(lane, j) : lane);
-    if (upd) y -= l * yj;
-  }
-  const double D = __shfl_sync(M, a, lane < 6 ? low_lane(lane, lane) : lane);
-  double z = (lane < 6) ? y / D : 0.0;
+    for (int k = 0; k < 6; k++) xk[k] = __shfl_sync(M, x, k);
+    double res = 0.0;
+    if (lane < 6) {
+      res = fin[21 + lane];
 #pragma unroll
-  for (int j = 5; j >= 0; j--) {
-    const double xj = __shfl_sync(M, z, j);
-    const bool upd = lane < j;
-    const double l = __shfl_sync(M, a, upd ? low_lane(j, lane) : lane);
-    if (upd) z -= l * xj;
+      for (int k = 0; k < 6; k++) res -= fin[lane <= k ? tri_index(lane, k) : tri_index(k, lane)] * xk[k];
+    }
+    float dv = (float)res;
+    warp_ldl_solve_f32(a, a, lane, r, c, dv);
+    if (lane < 6) x += (double)dv;
   }
-  x = z;
-  return nanp ? 2 : 0;
+  return 0;
 }
 
-// SE(3) exponential in the reference's parameterisation
+// SE(3) exponential of the twist [w; v] in the reference's parameterisation
 // (z_uitme_Update_Incremental_Tracking_with_Matrix_Exponential,
-// z_yooji_cuda_pose_tracker.cu:50-149): with th = |w| and u = w / th,
-// R = I + sin(th)[u]x + (1 - cos(th))[u]x^2 and
-// t = (I - R)[u]x v / th + u u^T v; [u]x^2 = u u^T - I.  For th < 0.1 sin and
-// 1 - cos come from their Taylor series (through th^11 and th^12, truncation
-// below 1e-20 relative); below th = 1e-10 the first-order limit R = I + [w]x,
-// t = v is used (the reference divides by th unguarded).  Lane l < 16 returns
-// element l of the 4x4 result; x is lane i's twist component.
+// z_yooji_cuda_pose_tracker.cu:50-149: R = I + sin(th)[u]x +
+// (1 - cos(th))[u]x^2 with u = w / th, t = (I - R)[u]x v / th + u u^T v),
+// written with W = [w]x as R = I + A W + B W^2, t = v + B (w x v) +
+// C (w (w.v) - th^2 v), A = sin(th)/th, B = (1 - cos(th))/th^2,
+// C = (th - sin(th))/th^3 - the same function, with no division by th.  For
+// th < 0.1 the three coefficients come from their Taylor series in th^2
+// (truncation below 1e-17 relative), one per lane; otherwise from sin/cos.
+// Lane l < 16 returns element l of the 4x4 result; x is lane i's component.
 __device__ double warp_se3_exp(double x, int lane) {
   const unsigned M = 0xffffffffu;
   double q[6];
 #pragma unroll
   for (int k = 0; k < 6; k++) q[k] = __shfl_sync(M, x, k);
+  const double th2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+  double coef = 0.0;
+  if (th2 < 0.01) {
+    const double t = th2;
+    if (lane == 0)  // sin(th)/th
+      coef = 1.0 - t * (1.0 / 6.0) * (1.0 - t * (1.0 / 20.0) * (1.0 - t * (1.0 / 42.0) * (1.0 - t * (1.0 / 72.0) * (1.0 - t * (1.0 / 110.0)))));
+    else if (lane == 1)  // (1 - cos(th))/th^2
+      coef = 0.5 * (1.0 - t * (1.0 / 12.0) * (1.0 - t * (1.0 / 30.0) * (1.0 - t * (1.0 / 56.0) * (1.0 - t * (1.0 / 90.0) * (1.0 - t * (1.0 / 132.0))))));
+    else if (lane == 2)  // (th - sin(th))/th^3
+      coef = (1.0 / 6.0) * (1.0 - t * (1.0 / 20.0) * (1.0 - t * (1.0 / 42.0) * (1.0 - t * (1.0 / 72.0) * (1.0 - t * (1.0 / 110.0) * (1.0 - t * (1.0 / 156.0))))));
+  } else if (lane < 3) {
+    const double th = sqrt(th2);
+    const double sn = sin(th), cs = cos(th);
+    coef = (lane == 0) ? sn / th : (lane == 1) ? (1.0 - cs) / th2 : (th - sn) / (th2 * th);
+  }
+  const double A = __shfl_sync(M, coef, 0), B = __shfl_sync(M, coef, 1), C = __shfl_sync(M, coef, 2);
   const int r = (lane >> 2) & 3, cc = lane & 3;
   if (lane >= 16 || r == 3) return (lane == 15) ? 1.0 : 0.0;
-  const double th2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-  const double th = sqrt(th2);
-  if (th < 1e-10) {
-    const double wx[9] = {0.0, -q[2], q[1], q[2], 0.0, -q[0], -q[1], q[0], 0.0};
-    if (cc == 3) return q[3 + r];
-    return (r == cc ? 1.0 : 0.0) + wx[r * 3 + cc];
+  const double W[9] = {0.0, -q[2], q[1], q[2], 0.0, -q[0], -q[1], q[0], 0.0};
+  if (cc < 3) {
+    const double dl = (r == cc) ? 1.0 : 0.0;
+    return dl + A * W[r * 3 + cc] + B * (q[r] * q[cc] - th2 * dl);
   }
-  double sn, cs;
-  if (th < 0.1) {
-    sn = th * (1.0 - th2 / 6.0 * (1.0 - th2 / 20.0 * (1.0 - th2 / 42.0 * (1.0 - th2 / 72.0 * (1.0 - th2 / 110.0)))));
-    cs = th2 / 2.0 *
-         (1.0 - th2 / 12.0 * (1.0 - th2 / 30.0 * (1.0 - th2 / 56.0 * (1.0 - th2 / 90.0 * (1.0 - th2 / 132.0)))));
-  } else {
-    sn = sin(th);
-    cs = 1.0 - cos(th);
-  }
-  const double it = 1.0 / th;
-  const double u[3] = {q[0] * it, q[1] * it, q[2] * it};
-  const double v[3] = {q[3] * it, q[4] * it, q[5] * it};
-  const double ux[9] = {0.0, -u[2], u[1], u[2], 0.0, -u[0], -u[1], u[0], 0.0};
-  double R[3];  // row r of R
-#pragma unroll
-  for (int k = 0; k < 3; k++) R[k] = (r == k ? 1.0 : 0.0) + sn * ux[r * 3 + k] + cs * (u[r] * u[k] - (r == k ? 1.0 : 0.0));
-  if (cc < 3) return R[cc];
-  const double uv[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2], u[0] * v[1] - u[1] * v[0]};
-  const double udv = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
-  double t = u[r] * udv * th;
-#pragma unroll
-  for (int k = 0; k < 3; k++) t += ((r == k ? 1.0 : 0.0) - R[k]) * uv[k];
-  return t;
+  const double wxv[3] = {q[1] * q[5] - q[2] * q[4], q[2] * q[3] - q[0] * q[5], q[0] * q[4] - q[1] * q[3]};
+  const double wv = q[0] * q[3] + q[1] * q[4] + q[2] * q[5];
+  return q[3 + r] + B * wxv[r] + C * (q[r] * wv - th2 * q[3 + r]);
 }
 
 // out = A * B (4x4, lane l < 16 computes element l); A in shared memory
@@ -389,17 +425,18 @@ __global__ void __launch_bounds__(kThreads, 3) k_icp_iter(const SessionDev* __re
 #pragma unroll
   for (int m = 16; m >= 1; m >>= 1) acc.shfl_add(m);
 
-  __shared__ double2 wsum[kThreads / 32][29];
+  typedef typename PartT<MODE>::type PT;
+  __shared__ PT wsum[kThreads / 32][29];
   __shared__ int s_last;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0)
 #pragma unroll
     for (int k = 0; k < 29; k++) wsum[warp][k] = acc.get(k);
   __syncthreads();
-  double2* part = reinterpret_cast<double2*>(s->partials) + (size_t)blockIdx.x * kPartials;
+  PT* part = reinterpret_cast<PT*>(s->partials) + (size_t)blockIdx.x * kPartials;
   if (threadIdx.x < 29) {
-    double2 v = wsum[0][threadIdx.x];
-    for (int q = 1; q < kThreads / 32; q++) v = combine<MODE>(v, wsum[q][threadIdx.x]);
+    PT v = wsum[0][threadIdx.x];
+    for (int q = 1; q < kThreads / 32; q++) v = combine(v, wsum[q][threadIdx.x], MODE);
     part[threadIdx.x] = v;
     __threadfence();
   }
@@ -418,19 +455,16 @@ __global__ void __launch_bounds__(kThreads, 3) k_icp_iter(const SessionDev* __re
     // 8 threads per quantity, each a fixed stride over blocks, then a fixed
     // shuffle tree
     const int k = threadIdx.x >> 3, j = threadIdx.x & 7;
-    double2 v = make_double2(0.0, 0.0);
+    PT v;
+    v.x = 0;
+    v.y = 0;
     if (k < 29) {
-      const double2* base = reinterpret_cast<const double2*>(s->partials);
-      for (int bb = j; bb < (int)gridDim.x; bb += 8) v = combine<MODE>(v, __ldcg(base + (size_t)bb * kPartials + k));
+      const PT* base = reinterpret_cast<const PT*>(s->partials);
+      for (int bb = j; bb < (int)gridDim.x; bb += 8) v = combine(v, __ldcg(base + (size_t)bb * kPartials + k), MODE);
     }
 #pragma unroll
-    for (int m = 4; m >= 1; m >>= 1) {
-      double2 o;
-      o.x = __shfl_xor_sync(0xffffffffu, v.x, m);
-      o.y = __shfl_xor_sync(0xffffffffu, v.y, m);
-      v = combine<MODE>(v, o);
-    }
-    if (k < 29 && j == 0) fin[k] = v.x + v.y;
+    for (int m = 4; m >= 1; m >>= 1) v = combine(v, shfl_xor2(v, m), MODE);
+    if (k < 29 && j == 0) fin[k] = (double)v.x + (double)v.y;
   }
   __syncthreads();
   if (threadIdx.x >= 32) return;
