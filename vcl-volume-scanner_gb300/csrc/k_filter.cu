@@ -189,9 +189,40 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
   if (warp != 0) return;
   const uint32_t M0 = 0x55555555u, M1 = 0xaaaaaaaau;
   const int wpl = (nw + 31) >> 5;  // words per lane (1 up to 1024 pixels, 2 up to 2048)
-  uint32_t rup[2] = {0u, 0u};      // this lane's words of the row above
-  uint32_t cout_prev = 0u;
   const int steps = L.h + 31;
+  if (wpl == 1) {
+    // both outcomes of a word are formed before its carry arrives, so a step's
+    // critical path is one shuffle and one select
+    const bool act = lane < nw;
+    uint32_t rup = 0u, cout = 0u;
+    for (int t = 0; t < steps; t++) {
+      const int row = t - lane;
+      const bool valid = act && row >= 0 && row < L.h;
+      uint32_t R0 = 0u, R1 = 0u;
+      if (valid && row > 0) {  // row 0 is never processed (interior rows only)
+        const uint32_t C = amask[row * nw + lane] & ~rup;
+        const uint32_t st = C & ~(C << 1);  // run starts (bit 0 counted as a start)
+        const uint32_t ev = (C & ((C + ((st & ~1u) & M0)) ^ C)) & M0;
+        const uint32_t od = (C & ((C + ((st & ~1u) & M1)) ^ C)) & M1;
+        // a run at bit 0 continues the previous word's alternation: even
+        // parity after a clear carry, odd after a set one
+        const uint32_t b0 = st & 1u;
+        R0 = ev | ((C & ((C + b0) ^ C)) & M0) | od;
+        R1 = ev | od | ((C & ((C + b0) ^ C)) & M1);
+      }
+      uint32_t cin = __shfl_up_sync(0xffffffffu, cout, 1);
+      if (lane == 0) cin = 0u;
+      const uint32_t R = cin ? R1 : R0;
+      if (valid) {
+        L.rmask[(size_t)row * nw + lane] = R;
+        rup = R;
+      }
+      cout = valid ? (R >> 31) : 0u;
+    }
+    return;
+  }
+  uint32_t rup[2] = {0u, 0u};  // this lane's words of the row above
+  uint32_t cout_prev = 0u;
   for (int t = 0; t < steps; t++) {
     uint32_t cin = __shfl_up_sync(0xffffffffu, cout_prev, 1);
     if (lane == 0) cin = 0u;
@@ -203,12 +234,10 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
         const int wi = lane * wpl + q;
         if (q < wpl && wi < nw) {
           uint32_t R = 0u;
-          if (row > 0) {  // row 0 is never processed (interior rows only)
+          if (row > 0) {
             const uint32_t C = amask[row * nw + wi] & ~rup[q];
-            const uint32_t st = C & ~(C << 1);  // run starts (bit 0 counted as a start)
+            const uint32_t st = C & ~(C << 1);
             const uint32_t rest = st & ~1u;
-            // runs starting at even / odd bits; a run at bit 0 continues the
-            // previous word's alternation, so its parity is the carry
             const uint32_t se = (rest & M0) | (cin ? 0u : (st & 1u));
             const uint32_t so = (rest & M1) | (cin ? (st & 1u) : 0u);
             R = ((C & ((C + se) ^ C)) & M0) | ((C & ((C + so) ^ C)) & M1);
