@@ -1,25 +1,41 @@
 #!/usr/bin/env python3
-"""Benchmark of the per-frame reconstruction path on GB300.
+"""Benchmark: batched serving vs the plain one-session-per-launch path.
 
-Workload ("plain method at VGA"): one scanning session, 640x480 uint16 depth
-frames (fx = fy = 525, cx = 319.5, cy = 239.5) from the seeded synthetic scene
-generator with Kinect-style axial noise, 1.5 % dropout in 8x8 blobs and a
-2.5 m cut-off; a 512^3 int16 TSDF + uint16 weight volume over 1.5 m,
-truncation 2 cm; ICP 10/5/4 iterations with a 10 cm distance and 20 degree
-normal rejection.  A step is one frame through vs_scan_frame: ingest, bilateral
-filter, pyramid, input vertex/normal maps, ICP, TSDF integration, ray-cast of
-three levels.
+Workload ("serving mix"): 64 scanning sessions, each with its own seeded
+synthetic scene (spheres/boxes on a ground plane, camera orbit of radius
+0.9 m, Kinect-style axial noise, 1.5 % dropout in 8x8 blobs, depth cut at
+2.5 m) and its own length drawn from U{50..500} frames.  Frame sizes cycle
+through 320x240 (fx = fy = 285), 512x424 (fx = fy = 365) and 640x480
+(fx = fy = 525); volumes are 128^3 to 512^3 int16 TSDF + uint16 weight over a
+1.5 m cube (at most 512 MiB each), truncation 2 cm, ICP 10/5/4 iterations with
+10 cm / 20 degree rejection, compensated (two-sum) reduction.
 
-  value   frames/s on the device: inputs resident in HBM, each frame timed
-          with CUDA events on its stream, L2 flushed (256 MB write) between
-          frames outside the timed events.
-  e2e     frames/s through the C ABI with host buffers: vs_scan_frame_host
-          copies the uint16 frame in and the pose out every frame.
+A step is one batched pass of the whole pipeline (ingest, bilateral filter,
+pyramid, input normal maps, ICP, integration, ray-cast of three levels) over
+the frame of every session that is still running: step r carries frame r of
+each session longer than r frames.
+
+  value      frames/s of the batched form: all frames resident in HBM, steps
+             enqueued back to back, CUDA events on the launching stream around
+             the timed steps.  The working set of a step (64 frames, the
+             active sub-cubes of 64 volumes, 13 GB of volumes in all) is far
+             larger than L2, so L2 is not flushed.
+  e2e        the same steps through the C ABI with host frames
+             (vs_batch_step_host: pinned uint16 frames in, poses out, every
+             step).
+  plain      the same frames through the plain path, one session per launch
+             (vs_scan_frame per frame, one graph per frame).
+  serving    open-loop arrivals through the serving loop (vs_server_*): every
+             session sends frames as a Poisson stream of 31.25 frames/s
+             (2000 frames/s aggregate while all 64 run), host frames in,
+             results polled out; latency = result on the host - scheduled
+             arrival.  The plain path serves the same arrival schedule
+             first-come first-served, one frame per launch.
 
 `--impl reference` times the CPU restatement of the reference's path (the
-reference itself does not build on Linux) on the host cores with all threads.
-Under torchrun every rank runs its own session (sessions are independent:
-replicas, weak scaling); rank 0 prints the JSON line.
+reference itself does not build on Linux) on the same session mix with all
+host threads.  Under torchrun every rank runs its own copy of the workload
+(sessions are independent: replicas, weak scaling); rank 0 prints the line.
 """
 import argparse
 import ctypes
@@ -28,6 +44,7 @@ import os
 import statistics
 import subprocess
 import sys
+import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -37,20 +54,24 @@ for _p in (os.path.join(ROOT, "vcl-volume-scanner_gb300"), os.path.join(ROOT, "o
 
 import numpy as np  # noqa: E402
 
-WORKLOAD = dict(name="plain_vga_512", width=640, height=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5,
-                volume=512, size_m=1.5, mu=0.02, icp_iters=(10, 5, 4), th_icp=0.1 ** 2, normal_deg=20.0,
-                dropout_blob=0.015, max_depth=2.5, seed=2, sequence_frames=300)
-L2_FLUSH_BYTES = 256 << 20
+MIX = dict(name="serving_mix_64", sessions=64, seed=5, length=(50, 500),
+           sizes=[(320, 240, 285.0, 160.0, 120.0), (512, 424, 365.0, 255.5, 211.5), (640, 480, 525.0, 319.5, 239.5)],
+           volumes=(128, 256, 384, 512), size_m=1.5, mu=0.02, icp_iters=(10, 5, 4), th_icp=0.1 ** 2,
+           normal_deg=20.0, dropout_blob=0.015, max_depth=2.5, arrival_fps=2000.0, hbm_budget_gb=150)
 
 
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=295)
+    ap.add_argument("--steps", type=int, default=500, help="batched steps (frames per session are capped at it)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sessions", type=int, default=MIX["sessions"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--ref-seconds", type=float, default=90.0, help="budget of the reference arm")
+    ap.add_argument("--ate-frames", type=int, default=12)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
     return ap.parse_args()
 
 
@@ -59,38 +80,74 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
-def make_frames(n, seed_offset=0):
+# ---------------------------------------------------------------------------
+# workload
+# ---------------------------------------------------------------------------
+def session_specs(n, max_len, seed):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n):
+        w, h, f, cx, cy = MIX["sizes"][i % 3]
+        dim = int(MIX["volumes"][int(rng.integers(0, len(MIX["volumes"])))])
+        length = int(min(max_len, rng.integers(MIX["length"][0], MIX["length"][1] + 1)))
+        specs.append(dict(w=w, h=h, f=f, cx=cx, cy=cy, dim=dim, length=max(1, length), seed=1000 + seed * 100 + i))
+    return specs
+
+
+def generate(spec):
     import vs_scanner as V
 
-    w = WORKLOAD
-    sc = V.synth_config(w["width"], w["height"], fx=w["fx"], fy=w["fy"], cx=w["cx"], cy=w["cy"], n_frames=n,
-                        seed=w["seed"] + seed_offset, dropout_blob=w["dropout_blob"], max_depth=w["max_depth"])
+    sc = V.synth_config(spec["w"], spec["h"], fx=spec["f"], fy=spec["f"], cx=spec["cx"], cy=spec["cy"],
+                        n_frames=spec["length"], seed=spec["seed"], dropout_blob=MIX["dropout_blob"],
+                        max_depth=MIX["max_depth"])
     depth, gt, centre = V.synth_generate(sc)
     return depth, gt, centre
 
 
-def make_config(centre):
+def make_config(spec, centre):
     import vs_scanner as V
 
-    w = WORKLOAD
-    origin, vox = V.cube_around(centre, w["size_m"], w["volume"])
-    return V.default_config(w["width"], w["height"], fx=w["fx"], fy=w["fy"], cx=w["cx"], cy=w["cy"],
-                            dim=(w["volume"],) * 3, origin=origin, voxel_size=vox, mu=w["mu"],
-                            th_icp=w["th_icp"], cos_normal=float(np.cos(np.radians(w["normal_deg"]))),
-                            icp_iters=w["icp_iters"], tsdf_type=V.VS_TSDF_INT16, reduce_mode=V.VS_REDUCE_KAHAN)
+    origin, vox = V.cube_around(centre, MIX["size_m"], spec["dim"])
+    return V.default_config(spec["w"], spec["h"], fx=spec["f"], fy=spec["f"], cx=spec["cx"], cy=spec["cy"],
+                            dim=(spec["dim"],) * 3, origin=origin, voxel_size=vox, mu=MIX["mu"],
+                            th_icp=MIX["th_icp"], cos_normal=float(np.cos(np.radians(MIX["normal_deg"]))),
+                            icp_iters=MIX["icp_iters"], tsdf_type=V.VS_TSDF_INT16, reduce_mode=V.VS_REDUCE_KAHAN)
 
 
-def config_json(args, world):
-    w = WORKLOAD
-    return {"workload": "%s: 1 session, %dx%d uint16 depth, %d^3 int16+uint16 TSDF over %.1f m, mu %.0f cm, "
-                        "ICP %d/%d/%d, 10 cm / 20 deg rejection" % (
-                            w["name"], w["width"], w["height"], w["volume"], w["size_m"], w["mu"] * 100,
-                            *w["icp_iters"]),
-            "frames": args.steps, "sessions_per_gpu": 1, "parallelism": "replicas x%d" % world,
-            "l2": "flushed between steps (256 MB write outside the timed events)",
-            "scene": "seeded synthetic spheres/boxes on a ground plane, orbit 0.9 m, seed %d" % w["seed"]}
+def build_workload(n, max_len, seed):
+    specs = session_specs(n, max_len, seed)
+    seqs = []
+    for sp in specs:
+        depth, gt, centre = generate(sp)
+        seqs.append(dict(spec=sp, depth=depth, gt=gt, centre=centre, cfg=make_config(sp, centre)))
+    return seqs
 
 
+def config_json(args, seqs, world):
+    lens = [s["spec"]["length"] for s in seqs]
+    sizes = {}
+    for s in seqs:
+        k = "%dx%d" % (s["spec"]["w"], s["spec"]["h"])
+        sizes[k] = sizes.get(k, 0) + 1
+    vols = {}
+    for s in seqs:
+        k = "%d^3" % s["spec"]["dim"]
+        vols[k] = vols.get(k, 0) + 1
+    return {"workload": "%s: %d sessions, lengths U{%d..%d} (capped at %d), frame sizes %s, volumes %s int16+uint16 "
+                        "over %.1f m, mu %.0f cm, ICP %d/%d/%d, 10 cm / 20 deg rejection, Poisson %.0f frames/s "
+                        "aggregate, HBM budget %d GB" % (
+                            MIX["name"], len(seqs), MIX["length"][0], MIX["length"][1], args.steps, sizes, vols,
+                            MIX["size_m"], MIX["mu"] * 100, *MIX["icp_iters"], MIX["arrival_fps"],
+                            MIX["hbm_budget_gb"]),
+            "frames": int(sum(lens)), "sessions_per_gpu": len(seqs), "parallelism": "replicas x%d" % world,
+            "l2": "not flushed: a step's working set (64 frames, active sub-cubes of 64 volumes) is far above L2",
+            "scene": "seeded synthetic spheres/boxes on a ground plane, orbit 0.9 m, session seeds 1000+%d*100+i"
+                     % MIX["seed"]}
+
+
+# ---------------------------------------------------------------------------
+# measurement helpers
+# ---------------------------------------------------------------------------
 def measured_peak_hbm():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     try:
@@ -164,86 +221,99 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(depth, centre, seconds, threads):
-    """The oracle (reference semantics, FP32, reference reduction tree) on a
-    bounded prefix of the same sequence."""
-    import oracle_py as O
-
-    lib = O.load()
-    del lib
-    try:
-        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(threads))
-    except OSError:
-        pass
-    cfg = make_config(centre)
-    ocfg = O.config_from_vs(cfg, reduce_mode=0)
-    s = O.Session(ocfg)
-    n = 0
-    t0 = time.perf_counter()
-    poses = []
-    while n < depth.shape[0]:
-        s.frame(depth[n])
-        poses.append(s.pose().astype(np.float64))
-        n += 1
-        if time.perf_counter() - t0 > seconds and n >= 2:
-            break
-    dt = time.perf_counter() - t0
-    return n / dt, n, dt, poses
-
-
-def fp64_trajectory(depth, centre, n, threads):
-    import oracle_py as O
-
-    try:
-        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(threads))
-    except OSError:
-        pass
-    cfg = make_config(centre)
-    s = O.Session(O.config_from_vs(cfg, reduce_mode=3, tsdf_store=0), f64=True)
-    out = []
-    for k in range(n):
-        s.frame(depth[k])
-        out.append(s.pose_f64())
-    return out
+def pct(a, q):
+    return float(np.percentile(np.asarray(a, np.float64), q)) if len(a) else None
 
 
 def centres(poses):
-    return np.array([-np.asarray(T)[:3, :3].T @ np.asarray(T)[:3, 3] for T in poses])
+    return np.array([-np.asarray(T, np.float64)[:3, :3].T @ np.asarray(T, np.float64)[:3, 3] for T in poses])
 
 
+def set_omp_threads(n):
+    try:
+        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(int(n))
+    except OSError:
+        pass
+
+
+def arrival_schedule(seqs, fps_total, seed):
+    """(t, session index, frame) sorted by t: each session a Poisson stream of
+    fps_total / n_sessions frames/s from t = 0"""
+    rng = np.random.default_rng(seed)
+    rate = fps_total / len(seqs)
+    ev = []
+    for i, s in enumerate(seqs):
+        gaps = rng.exponential(1.0 / rate, size=s["spec"]["length"])
+        t = np.cumsum(gaps)
+        ev += [(float(t[k]), i, k) for k in range(len(t))]
+    ev.sort()
+    return ev
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the CPU restatement on the same mix
+# ---------------------------------------------------------------------------
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return
-    n_threads = os.cpu_count() or 1
-    depth, gt, centre = make_frames(args.warmup + args.steps)
     import oracle_py as O
 
+    n_threads = os.cpu_count() or 1
     O.load()
-    try:
-        ctypes.CDLL("libgomp.so.1").omp_set_num_threads(n_threads)
-    except OSError:
-        pass
-    cfg = make_config(centre)
-    s = O.Session(O.config_from_vs(cfg, reduce_mode=0))
-    for k in range(args.warmup):
-        s.frame(depth[k])
-    times = []
-    for k in range(args.warmup, args.warmup + args.steps):
-        t0 = time.perf_counter()
-        s.frame(depth[k])
-        times.append(time.perf_counter() - t0)
+    set_omp_threads(n_threads)
+    specs = session_specs(args.sessions, args.steps, MIX["seed"])
+    # a bounded sample: the first frames of the first sessions (one of each
+    # size in turn), round robin, until the time budget or K frames
+    sample_sessions = min(6, len(specs))
+    seqs = []
+    for sp in specs[:sample_sessions]:
+        sp = dict(sp, length=min(sp["length"], 40))
+        depth, gt, centre = generate(sp)
+        seqs.append((O.Session(O.config_from_vs(make_config(sp, centre), reduce_mode=0)), depth))
+    for k in range(min(args.warmup, 2)):
+        for s, d in seqs:
+            s.frame(d[k])
+    times, n, k = [], 0, min(args.warmup, 2)
+    t_start = time.perf_counter()
+    while n < args.steps and time.perf_counter() - t_start < args.ref_seconds:
+        for s, d in seqs:
+            if k >= d.shape[0]:
+                continue
+            t0 = time.perf_counter()
+            s.frame(d[k])
+            times.append(time.perf_counter() - t0)
+            n += 1
+        k += 1
+        if all(k >= d.shape[0] for _, d in seqs):
+            break
     total = sum(times)
-    fps = args.steps / total
-    sample = "%d frames of the workload after %d warm-up frames, oracle port (reference FP32 semantics), %d threads" % (
-        args.steps, args.warmup, n_threads)
+    fps = len(times) / total
+    sample = ("%d frames: sessions 0..%d of the serving mix round robin (sizes 320x240/512x424/640x480), frames "
+              "%d.. of each, oracle port (reference FP32 semantics), %d threads" % (
+                  len(times), sample_sessions - 1, min(args.warmup, 2), n_threads))
     line = {"impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+            "steps": len(times), "warmup": min(args.warmup, 2), "ms_per_step": 1000.0 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-            "data": "synthetic", "config": config_json(args, 1),
+            "data": "synthetic", "config": {"workload": "%s (bounded CPU sample, see cpu_baseline.sample)" %
+                                                        MIX["name"]},
             "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": n_threads, "kind": "port", "sample": sample},
             "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+def stage_bytes(cfg, st):
+    """algorithmic bytes per frame and stage (st: active sub-cubes, voxels updated)"""
+    W, H = cfg.width, cfg.height
+    lv = [(W >> l) * (H >> l) for l in range(3)]
+    it = MIX["icp_iters"]
+    return {"filter": 6.0 * W * H + sum(lv[l] * (4 + 4 + 32) for l in range(3)),
+            "track": sum(28.0 * lv[l] * it[l] for l in range(3)),
+            "integrate": 4.0 * 512 * st[0] + 4.0 * st[1] + 2.0 * W * H + 8.0 * st[0],
+            "raycast": 28.0 * sum(lv)}
 
 
 def run_ours(args):
@@ -257,12 +327,6 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    n = args.warmup + args.steps
-    depth, gt, centre = make_frames(n, seed_offset=0)
-    cfg = make_config(centre)
-    frames_dev = torch.from_numpy(depth.view(np.int16)).cuda()
-    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    st = torch.cuda.Stream()
 
     def barrier():
         if world > 1:
@@ -271,152 +335,291 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    sess = V.Session(cfg)
-    sess.set_stage_timing(True)
-    kpf = sess.kernels_per_frame()
-    frame_bytes = cfg.width * cfg.height * 2
+    t_gen = time.perf_counter()
+    seqs = build_workload(args.sessions, args.steps, MIX["seed"])
+    t_gen = time.perf_counter() - t_gen
+    n_s = len(seqs)
+    lens = [s["spec"]["length"] for s in seqs]
+    rounds = max(lens)
+    n_frames = int(sum(lens))
+    frames_dev = [torch.from_numpy(s["depth"].view(np.int16)).cuda() for s in seqs]
+    pinned = [torch.from_numpy(s["depth"].view(np.int16)).pin_memory() for s in seqs]
+    host = [p.numpy().view(np.uint16) for p in pinned]
+    st = torch.cuda.Stream()
 
-    # ---- warm-up (untimed) ----
-    with torch.cuda.stream(st):
-        for k in range(args.warmup):
-            flush.zero_()
-            sess.scan_frame(frames_dev[k].data_ptr(), st.cuda_stream)
-    st.synchronize()
+    sessions = [V.Session(s["cfg"]) for s in seqs]
+    batch = V.Batch()
 
-    # ---- timed region: K frames, device events per frame ----
+    # ---- warm-up: graph capture and first launches on throwaway sessions ----
+    warm = [V.Session(seqs[i]["cfg"]) for i in range(min(4, n_s))]
+    for k in range(args.warmup):
+        batch.step(warm, [frames_dev[i][min(k, lens[i] - 1)].data_ptr() for i in range(len(warm))],
+                   st.cuda_stream)
+    batch.sync()
+    for w in warm:
+        w.close()
+
+    # ---- batched form, device-resident frames: the timed region ----
+    members = [[i for i in range(n_s) if lens[i] > r] for r in range(rounds)]
+    handles = [[sessions[i] for i in m] for m in members]
+    ptrs = [[frames_dev[i][r].data_ptr() for i in m] for r, m in enumerate(members)]
     clk = ClockSampler(local)
     barrier()
     clk.start()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    stage = np.zeros((args.steps, 4))
-    stats = np.zeros((args.steps, 4))
-    poses = []
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(rounds + 1)]
     t_wall = time.perf_counter()
-    with torch.cuda.stream(st):
-        for i in range(args.steps):
-            k = args.warmup + i
-            flush.zero_()
-            ev[i][0].record(st)
-            sess.scan_frame(frames_dev[k].data_ptr(), st.cuda_stream)
-            ev[i][1].record(st)
-            stage[i] = sess.stage_times()
-            stats[i] = sess.frame_stats()
+    ev[0].record(st)
+    for r in range(rounds):
+        batch.step(handles[r], ptrs[r], st.cuda_stream)
+        ev[r + 1].record(st)
     st.synchronize()
     t_wall = time.perf_counter() - t_wall
     barrier()
     clocks = clk.stop()
-    frame_ms = np.array([a.elapsed_time(b) for a, b in ev])
-    _, T64, info = sess.pose()
-    total_ms = float(frame_ms.sum())
+    step_ms = np.array([ev[r].elapsed_time(ev[r + 1]) for r in range(rounds)])
+    total_ms = float(ev[0].elapsed_time(ev[rounds]))
     if world > 1:
         import torch.distributed as dist
 
         t = torch.tensor([total_ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total_ms = float(t.item())
-    fps = world * args.steps / (total_ms / 1000.0)
+    fps_batched = world * n_frames / (total_ms / 1000.0)
+    kps = batch.kernels_per_step()
+    tracked_batched = [int(s.pose()[2][0]) for s in sessions]
+    final_batched = [s.pose()[1] for s in sessions]
 
-    # ---- end to end through the C ABI with host buffers ----
-    sess.set_stage_timing(False)
-    sess.reset()
-    pinned = torch.from_numpy(depth.view(np.int16)).pin_memory()
-    host = pinned.numpy().view(np.uint16)
-    e2e_poses = []
-    for k in range(args.warmup):
-        flush.zero_()
-        torch.cuda.synchronize()
-        sess.scan_frame_host(host[k])
+    # ---- stage breakdown of full steps (separate, synchronous pass) ----
+    for s in sessions:
+        s.reset()
+    batch.set_stage_timing(True)
+    n_stage = min(20, rounds)
+    stage = np.zeros((n_stage, 4))
+    alg = {k: 0.0 for k in ("filter", "track", "integrate", "raycast")}
+    for r in range(n_stage):
+        batch.step(handles[r], ptrs[r], st.cuda_stream)
+        batch.sync()
+        stage[r] = batch.stage_times()
+        for i in members[r]:
+            fs = sessions[i].frame_stats()
+            for k, v in stage_bytes(seqs[i]["cfg"], fs).items():
+                alg[k] += v
+    batch.set_stage_timing(False)
+    names = ["filter", "track", "integrate", "raycast"]
+    stage_sum = stage.sum(axis=0)
+    stage_mean = stage.mean(axis=0)
+
+    # ---- e2e: the same steps with host frames through the C ABI ----
+    for s in sessions:
+        s.reset()
+    batch.sync()
+    e2e_poses = {i: [] for i in range(min(3, n_s))}
     barrier()
-    e2e_t = []
-    for i in range(args.steps):
-        k = args.warmup + i
-        flush.zero_()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        T, tracked = sess.scan_frame_host(host[k])
-        e2e_t.append(time.perf_counter() - t0)
-        e2e_poses.append(T.astype(np.float64))
-    barrier()
-    e2e_total = sum(e2e_t)
+    t0 = time.perf_counter()
+    for r in range(rounds):
+        T, _ = batch.step_host(handles[r], [host[i][r] for i in members[r]])
+        for j, i in enumerate(members[r]):
+            if i in e2e_poses and len(e2e_poses[i]) < args.ate_frames:
+                e2e_poses[i].append(T[j].astype(np.float64))
+    e2e_s = time.perf_counter() - t0
     if world > 1:
         import torch.distributed as dist
 
-        t = torch.tensor([e2e_total], device="cuda", dtype=torch.float64)
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
-    e2e_fps = world * args.steps / e2e_total
+        e2e_s = float(t.item())
+    fps_e2e = world * n_frames / e2e_s
+    h2d = int(round(sum(h.nbytes for h in host) / rounds))  # mean host frame bytes per step
+    d2h = 64 * 80  # pose heads of every slot, one copy per step
+
+    # ---- plain path: one session per launch, same frames ----
+    for s in sessions:
+        s.reset()
+    torch.cuda.synchronize()
+    pev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    barrier()
+    pev[0].record(st)
+    with torch.cuda.stream(st):
+        for r in range(rounds):
+            for i in members[r]:
+                sessions[i].scan_frame(frames_dev[i][r].data_ptr(), st.cuda_stream)
+    pev[1].record(st)
+    st.synchronize()
+    plain_ms = float(pev[0].elapsed_time(pev[1]))
+    fps_plain = world * n_frames / (plain_ms / 1000.0)
+    # the batched and plain runs of every session end on the same FP64 pose
+    plain_equal = all(np.array_equal(sessions[i].pose()[1], final_batched[i]) for i in range(n_s))
+
+    # ---- serving: open-loop Poisson arrivals ----
+    serving = None
+    plain_serving = None
+    if not args.no_serving:
+        sched = arrival_schedule(seqs, MIX["arrival_fps"], MIX["seed"] + 17)
+        serving = run_serving(V, seqs, host, sched)
+        for s in sessions:
+            s.reset()
+        plain_serving = run_plain_serving(sessions, host, sched)
+    batch.close()
+    for s in sessions:
+        s.close()
 
     if rank != 0:
         return
-    # ---- roofline of the dominant stage ----
-    stage_mean = stage.mean(axis=0)
-    names = ["filter", "track", "integrate", "raycast"]
     peak, peak_kind = measured_peak_hbm()
-    W, H = cfg.width, cfg.height
-    active, nupd = stats[:, 0].mean(), stats[:, 1].mean()
-    # algorithmic bytes per launch (one frame):
-    #   integrate: 4 B per swept voxel pair (512 per active sub-cube) read,
-    #              4 B per updated voxel written, 2 B per depth pixel, 8 B of
-    #              flag + list per active sub-cube
-    b_int = 4.0 * 512 * active + 4.0 * nupd + 2.0 * W * H + 8.0 * active
-    lv = [(W >> l) * (H >> l) for l in range(3)]
-    iters = WORKLOAD["icp_iters"]
-    b_icp = sum(28.0 * lv[l] * iters[l] for l in range(3))
-    b_filter = 6.0 * W * H + sum(lv[l] * (4 + 4 + 32) for l in range(3))
-    b_ray = 28.0 * sum(lv)
-    alg = {"filter": b_filter, "track": b_icp, "integrate": b_int, "raycast": b_ray}
-    dom = names[int(np.argmax(stage_mean))]
-    achieved = alg[dom] / (stage_mean[names.index(dom)] * 1e-3) / 1e9
+    dom_i = int(np.argmax(stage_sum))
+    dom = names[dom_i]
+    achieved = {k: alg[k] / (stage_sum[names.index(k)] * 1e-3) / 1e9 for k in names}
     kernel_key = {"integrate": "k_integrate", "raycast": "k_raycast", "track": "k_icp_iter",
-                  "filter": "k_bilateral"}[dom]
-    traffic = traffic_from_profiles(kernel_key)
-    roofline = {"bound": "hbm", "kernel": kernel_key, "stage": dom, "achieved": achieved, "peak": peak,
-                "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
-                "peak_source": "%s (MEASURED_PEAKS.json hbm_gbs)" % peak_kind if peak_kind == "measured" else
+                  "filter": "k_bilateral_batch"}[dom]
+    roofline = {"bound": "hbm", "kernel": kernel_key, "stage": dom, "achieved": achieved[dom], "peak": peak,
+                "unit": "GB/s", "frac": achieved[dom] / peak, "traffic": traffic_from_profiles(kernel_key),
+                "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6800 GB/s",
-                "note": "algorithmic bytes of the stage per frame / its event-timed duration"}
-    integ = {"achieved_gbs": b_int / (stage_mean[2] * 1e-3) / 1e9, "frac": b_int / (stage_mean[2] * 1e-3) / 1e9 / peak,
-             "active_subcubes": active, "voxels_updated": nupd, "algorithmic_bytes": b_int}
+                "note": "algorithmic bytes of the stage over the sessions of %d full steps / its event-timed "
+                        "duration" % n_stage,
+                "stages_gbs": achieved, "stages_frac": {k: v / peak for k, v in achieved.items()}}
 
-    # ---- CPU baseline and FP64 trajectory check on a bounded prefix ----
     cpu = None
     ate = None
     if not args.no_cpu:
-        fps_cpu, ncpu, tcpu, cpu_poses = cpu_baseline(depth, centre, args.cpu_seconds, 1)
-        cpu = {"value": fps_cpu, "unit": "frames/s", "cores": 1, "kind": "port",
-               "sample": "first %d frames of the same sequence (%.1f s), oracle port, reference FP32 semantics, "
-                         "1 thread" % (ncpu, tcpu)}
-        nf = min(ncpu, len(e2e_poses) + args.warmup)
-        ref64 = fp64_trajectory(depth, centre, nf, os.cpu_count() or 1)
-        # the e2e run restarted from frame 0 after reset: frames 0..warmup-1 untimed
-        ours = []
-        sess2 = V.Session(cfg)
-        for k in range(nf):
-            T, _ = sess2.scan_frame_host(host[k])
-            ours.append(T.astype(np.float64))
-        sess2.close()
-        d = np.linalg.norm(centres(ours) - centres(ref64), axis=1)
-        ate = {"vs_fp64_oracle_mm": float(np.sqrt(np.mean(d ** 2)) * 1e3), "frames": nf,
-               "max_mm": float(d.max() * 1e3)}
-    gt_err = np.linalg.norm(centres([gt[args.warmup + args.steps - 1]]) - centres([T64]), axis=1)[0]
+        cpu = cpu_baseline(seqs, args.cpu_seconds)
+        ate = ate_vs_fp64(seqs, e2e_poses, args.ate_frames)
 
-    line = {"metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": float(frame_ms.mean()), "higher_is_better": True,
+    line = {"metric": "frames/s", "value": fps_batched, "unit": "frames/s", "n_gpus": world, "steps": rounds,
+            "warmup": args.warmup, "ms_per_step": float(step_ms.mean()), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": config_json(args, world),
-            "latency_ms": {"p50": float(np.percentile(frame_ms, 50)), "p99": float(np.percentile(frame_ms, 99)),
-                           "max": float(frame_ms.max())},
-            "stages_ms": {n_: float(v) for n_, v in zip(names, stage_mean)},
-            "roofline": roofline, "integrate": integ,
+            "config": config_json(args, seqs, world),
+            "frames_per_step": n_frames / rounds,
+            "step_ms": {"p50": pct(step_ms, 50), "p99": pct(step_ms, 99), "max": float(step_ms.max())},
+            "plain": {"value": fps_plain, "unit": "frames/s", "ms": plain_ms,
+                      "note": "one session per launch (vs_scan_frame), same frames, device-resident",
+                      "final_poses_equal_batched": bool(plain_equal)},
+            "batched_over_plain": fps_batched / fps_plain,
+            "serving": serving, "plain_serving": plain_serving,
+            "stages_ms_per_step": {n_: float(v) for n_, v in zip(names, stage_mean)},
+            "roofline": roofline,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": frame_bytes,
-                    "d2h_bytes_per_step": 80},
-            "gpu_launches": int(kpf * args.steps),
+            "e2e": {"value": fps_e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "note": "vs_batch_step_host per step: pinned host frames in, pose heads out"},
+            "gpu_launches": int(kps * rounds),
             "clocks": clocks,
             "ate": ate,
-            "tracking": {"last_frame_tracked": int(info[0]), "camera_err_vs_generator_mm": float(gt_err * 1e3)},
-            "wall_s_timed_region": t_wall}
+            "tracked_last_frame": int(sum(tracked_batched)),
+            "generation_s": t_gen, "wall_s_timed_region": t_wall}
     print(json.dumps(line), flush=True)
+
+
+def run_serving(V, seqs, host, sched):
+    """open-loop arrivals through vs_server; latency from the scheduled arrival"""
+    srv = V.Server(hbm_budget=MIX["hbm_budget_gb"] << 30)
+    ids = [srv.open(s["cfg"]) for s in seqs]
+    results = []
+    done = threading.Event()
+
+    def poller():
+        while not done.is_set():
+            results.extend(srv.poll(timeout_ms=50))
+        while True:
+            got = srv.poll(timeout_ms=0)
+            if not got:
+                break
+            results.extend(got)
+
+    th = threading.Thread(target=poller)
+    th.start()
+    t0 = srv.clock() + 0.05
+    busy = 0
+    try:
+        for t, i, k in sched:
+            while True:
+                now = srv.clock()
+                if now >= t0 + t:
+                    break
+                time.sleep(min(0.0005, t0 + t - now))
+            while not srv.submit(ids[i], host[i][k]):
+                busy += 1
+                time.sleep(0.0002)
+        srv.drain()
+    finally:
+        done.set()
+        th.join()
+    stats = srv.stats()
+    srv.close()
+    arr = {(i, k): t0 + t for t, i, k in sched}
+    lat = [1000.0 * (r["t_done"] - arr[(ids.index(r["session"]), r["frame"])]) for r in results]
+    t_first = t0 + sched[0][0]
+    t_last = max(r["t_done"] for r in results)
+    span_arr = sched[-1][0] - sched[0][0]
+    return {"offered_fps_peak": MIX["arrival_fps"], "offered_fps_mean": len(sched) / span_arr,
+            "frames": len(results), "achieved_fps": len(results) / (t_last - t_first),
+            "span_s": t_last - t_first, "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "max_ms": float(max(lat)),
+            "mean_batch": stats["mean_batch"], "max_batch": stats["max_batch_seen"], "steps": stats["steps"],
+            "submit_retries": busy, "sessions_admitted": len(ids),
+            "hbm_resident_gb": stats["bytes_resident"] / 2 ** 30 if stats["bytes_resident"] else None}
+
+
+def run_plain_serving(sessions, host, sched):
+    """the same arrivals served first-come first-served, one frame per launch"""
+    lat = []
+    t0 = time.perf_counter() + 0.05
+    for t, i, k in sched:
+        now = time.perf_counter()
+        if now < t0 + t:
+            time.sleep(t0 + t - now)
+        sessions[i].scan_frame_host(host[i][k])
+        lat.append(1000.0 * (time.perf_counter() - (t0 + t)))
+    span = time.perf_counter() - (t0 + sched[0][0])
+    return {"offered_fps_peak": MIX["arrival_fps"], "frames": len(lat), "achieved_fps": len(lat) / span,
+            "p50_ms": pct(lat, 50), "p99_ms": pct(lat, 99), "max_ms": float(max(lat))}
+
+
+def cpu_baseline(seqs, seconds):
+    """The oracle (reference semantics, FP32, reference reduction tree), one
+    thread, on a bounded sample: the first frames of sessions 0..2 (one of
+    each frame size), round robin."""
+    import oracle_py as O
+
+    O.load()
+    set_omp_threads(1)
+    ss = [(O.Session(O.config_from_vs(seqs[i]["cfg"], reduce_mode=0)), seqs[i]["depth"]) for i in range(min(3, len(seqs)))]
+    n, k = 0, 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds or n < 3:
+        progressed = False
+        for s, d in ss:
+            if k < d.shape[0]:
+                s.frame(d[k])
+                n += 1
+                progressed = True
+        k += 1
+        if not progressed:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
+            "sample": "%d frames (first %d of sessions 0..2: 320x240, 512x424, 640x480), %.1f s, oracle port, "
+                      "reference FP32 semantics, 1 thread" % (n, k, dt)}
+
+
+def ate_vs_fp64(seqs, poses, nf):
+    """RMS camera-centre error of the batched poses against the FP64 oracle
+    run of the same frames (both trajectories start at the identity)"""
+    import oracle_py as O
+
+    set_omp_threads(os.cpu_count() or 1)
+    out = {}
+    worst = 0.0
+    for i, ours in poses.items():
+        s = O.Session(O.config_from_vs(seqs[i]["cfg"], reduce_mode=3, tsdf_store=0), f64=True)
+        ref = []
+        for k in range(len(ours)):
+            s.frame(seqs[i]["depth"][k])
+            ref.append(s.pose_f64())
+        d = np.linalg.norm(centres(ours) - centres(ref), axis=1)
+        rms = float(np.sqrt(np.mean(d ** 2)) * 1e3)
+        out["session_%d_%dx%d" % (i, seqs[i]["spec"]["w"], seqs[i]["spec"]["h"])] = {"rms_mm": rms, "frames": len(ours),
+                                                                                       "max_mm": float(d.max() * 1e3)}
+        worst = max(worst, rms)
+    return {"vs_fp64_oracle_mm": worst, "sessions": out}
 
 
 def main():

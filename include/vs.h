@@ -38,6 +38,9 @@ extern "C" {
 #define VS_ERR_CUDA (-2)    /* CUDA runtime failure / no device              */
 #define VS_ERR_STATE (-3)   /* call out of order                             */
 #define VS_ERR_MEMORY (-4)  /* device allocation failed                      */
+#define VS_ERR_BUSY (-5)    /* queue full / budget exhausted; retry later     */
+
+#define VS_MAX_BATCH 64     /* sessions advanced by one batched step          */
 
 /* TSDF storage of the volume (the reference stores float + uchar weight) */
 #define VS_TSDF_INT16 0     /* int16 q = rint(tsdf*32767), uint16 weight      */
@@ -217,6 +220,109 @@ int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, const float
                                float voxel_size, float mu, float max_w, const float* map_depth_dev,
                                int ww, int hh, const float* K, const float* T_gc_dev,
                                const float* T_cg_dev, void* stream);
+
+/* ---- batched frames ------------------------------------------------------
+ * A batch runner advances several sessions by one frame each with ONE launch
+ * per stage: every per-frame kernel is persistent over the work items of all
+ * sessions of a device-resident table, so the runner captures one CUDA graph
+ * and replays it for any set of sessions (sizes, volumes and levels may
+ * differ; reduce_mode and tsdf_type must agree).  Each session's items and
+ * their summation order are those it has alone, so a session's poses,
+ * volume and maps are identical whether it runs alone (vs_scan_frame) or in
+ * any batch.  The reference has one session per process and no batching;
+ * the step replaces n calls of so_Scan_Object's per-frame body
+ * (z_yooji_object_scanner.cpp:501-597).
+ *
+ * A session must not be used by two runners, or by its own entry points, while
+ * a step that includes it is in flight; vs_batch_sync() ends all of them. */
+typedef struct vs_batch vs_batch;
+
+int vs_batch_create(vs_batch** out);
+int vs_batch_destroy(vs_batch* b);
+/* one frame for each of n (1..VS_MAX_BATCH) distinct sessions.
+ * depth_mm_dev[i]: device uint16 frame of session i, or NULL (or a NULL
+ * array) when the frame is already in the session's input buffer.  Enqueued
+ * on `stream` (NULL: the runner's own stream); returns without waiting. */
+int vs_batch_step(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_dev,
+                  void* stream);
+/* host frames in, poses out (T_gc_out: n x 16 floats, tracked_out: n ints,
+ * either may be NULL); returns when the step has finished */
+int vs_batch_step_host(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_host,
+                       float* T_gc_out, int* tracked_out);
+int vs_batch_sync(vs_batch* b);
+/* stage events inside the batch graph; ms[4] as vs_get_stage_times, for the
+ * last finished step */
+int vs_batch_set_stage_timing(vs_batch* b, int enable);
+int vs_batch_get_stage_times(vs_batch* b, float* ms);
+/* kernels one step launches (the same for every batch size) */
+int vs_batch_kernels_per_step(vs_batch* b);
+
+/* ---- serving ---------------------------------------------------------------
+ * A server takes frames from many sessions as they arrive and runs them with
+ * continuous batching: a worker thread forms each step from the sessions that
+ * have a frame waiting (one frame per session per step, oldest first, round
+ * robin), launches it through a batch runner while the previous step is still
+ * on the GPU (two steps in flight), and a completion thread timestamps each
+ * frame's result.  Every session's volume, pose and maps stay on the device
+ * between frames.  Sessions are admitted while the resident set fits the HBM
+ * budget (vs_session_bytes of each) and a resident slot is free; a session
+ * that does not fit yet waits, queues its frames, and is admitted when closed
+ * sessions free memory.  Results equal those of the session run alone. */
+typedef struct vs_server vs_server;
+
+typedef struct {
+  size_t hbm_budget;        /* device bytes resident sessions may hold (0: 150 GB) */
+  int max_resident;         /* resident sessions, 1..VS_MAX_BATCH (0: VS_MAX_BATCH) */
+  int max_batch;            /* sessions per step, 1..VS_MAX_BATCH (0: VS_MAX_BATCH) */
+  int queue_depth;          /* frames buffered per session, 1..256 (0: 8)    */
+  int pipeline;             /* steps in flight, 1..2 (0: 2)                  */
+} vs_server_config;
+
+typedef struct {
+  int session;              /* id from vs_server_open                         */
+  int frame;                /* 0-based index of the frame in its session      */
+  int tracked;
+  int batch;                /* sessions in the step that ran the frame        */
+  float T_gc[16];
+  double t_submit;          /* seconds, vs_server_clock() time base           */
+  double t_done;            /* result on the host                             */
+  double latency_ms;
+} vs_result;
+
+typedef struct {
+  uint64_t steps, frames;
+  double mean_batch;
+  int max_batch_seen;
+  int resident, waiting, closed;
+  size_t bytes_resident, bytes_budget;
+} vs_server_stats;
+
+#define VS_SESSION_WAITING 0
+#define VS_SESSION_RESIDENT 1
+#define VS_SESSION_CLOSED 2
+
+void vs_server_config_default(vs_server_config* c);
+int vs_server_create(const vs_server_config* c, vs_server** out);
+/* finishes every queued frame, then frees all sessions */
+int vs_server_destroy(vs_server* s);
+/* VS_ERR_MEMORY when the session alone exceeds the budget */
+int vs_server_open(vs_server* s, const vs_config* cfg, int* id);
+int vs_server_state(vs_server* s, int id, int* state);
+/* copies the frame (width x height uint16) into the session's queue;
+ * VS_ERR_BUSY when queue_depth frames are already waiting */
+int vs_server_submit(vs_server* s, int id, const uint16_t* depth_mm_host);
+/* the session leaves after its queued frames; its memory admits waiters */
+int vs_server_close(vs_server* s, int id);
+/* up to max results, waiting at most timeout_ms for the first; returns the
+ * count (>= 0) or a VS_ERR_* code */
+int vs_server_poll(vs_server* s, vs_result* out, int max, int timeout_ms);
+/* waits until every submitted frame has finished */
+int vs_server_drain(vs_server* s);
+/* the resident session behind an id (state access; call after a drain) */
+int vs_server_get_session(vs_server* s, int id, vs_session** out);
+int vs_server_get_stats(vs_server* s, vs_server_stats* st);
+/* seconds on the monotonic clock of t_submit / t_done */
+double vs_server_clock(void);
 
 #ifdef __cplusplus
 }

@@ -1,13 +1,17 @@
 // Depth ingest, bilateral filter, depth pyramid and input vertex/normal maps.
 //
 // HBM-bound streaming stages: one pass over the uint16 frame, shared-memory
-// tiles with halos, coalesced 2D blocks.  Each kernel restates one reference
-// routine (paths relative to VCL_Volume_Scanner/):
-//   k_bilateral      d_bilateral_filter  STAC/Engine/GPU/z_yooji_cuda_img_proc.cu:103-141
-//   k_pyramid_down   sdg5 + ddh          STAC/Engine/CPU/z_yooji_image_processor.cpp:567-596,857-937
+// tiles with halos, coalesced 2D blocks.  Every kernel is persistent over the
+// tiles of all sessions of a batch table (one session = a table of one).
+// Each kernel restates one reference routine (paths relative to
+// VCL_Volume_Scanner/):
+//   k_bilateral_*    d_bilateral_filter  STAC/Engine/GPU/z_yooji_cuda_img_proc.cu:103-141
+//   k_pyramid_batch  sdg5 + ddh          STAC/Engine/CPU/z_yooji_image_processor.cpp:567-596,857-937
 //   k_inmap_*        cpm + enm           STAC/Engine/CPU/z_yooji_image_processor.cpp:119-227
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <cstring>
 
 #include "vs_internal.cuh"
 
@@ -15,19 +19,41 @@ namespace vs {
 namespace {
 
 constexpr int BX = 32, BY = 8;  // output tile of the bilateral filter
+constexpr int kScanSmem = 64 * 1024;  // staged normal-rejection bitmasks of one level
 
 // The reference reads a linear-filtered texture at integer coordinates, so
 // every tap is the mean of the 2x2 texels (X-1..X, Y-1..Y); out-of-range texel
 // coordinates clamp to the edge.  A tile of BX x BY outputs needs taps
 // X in [x0-2, x0+BX+1] and texels in [x0-3, x0+BX+1].
+struct BilateralSmem {
+  float tex[BY + 5][BX + 6];
+  float tap[BY + 4][BX + 5];
+};
+
+__device__ inline float bilateral_px(const BilateralSmem& m, int tx, int ty, const float g[5]) {
+  const float denom = 2.0f * 0.1f * 0.1f;  // 2 sigma_r^2, sigma_r = 0.1 m (z_yooji_cuda_img_proc.cu:44,91)
+  const float center = m.tap[ty + 2][tx + 2];
+  float t = 0.0f, sum = 0.0f;
+#pragma unroll
+  for (int i = -2; i <= 2; i++) {
+#pragma unroll
+    for (int j = -2; j <= 2; j++) {
+      float cur = m.tap[ty + 2 + i][tx + 2 + j];
+      if (cur <= 0.0f) return 0.0f;
+      float mod = (center - cur) * (center - cur);
+      float factor = g[i + 2] * g[j + 2] * __expf(-mod / denom);
+      t += factor * cur;
+      sum += factor;
+    }
+  }
+  return t / sum;
+}
+
+// one BX x BY output tile; the block's threads all take part (two barriers)
 template <bool FROM_MM>
-__global__ void __launch_bounds__(BX* BY)
-    k_bilateral(const uint16_t* __restrict__ mm, const float* __restrict__ fin, float scale,
-                float* __restrict__ raw_out, float* __restrict__ out, int W, int H, float g0,
-                float g1, float g2) {
-  __shared__ float tex[BY + 5][BX + 6];
-  __shared__ float tap[BY + 4][BX + 5];
-  const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
+__device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restrict__ mm,
+                                      const float* __restrict__ fin, float scale, float* __restrict__ raw_out,
+                                      float* __restrict__ out, int W, int H, int x0, int y0, const float g[5]) {
   const int tid = threadIdx.y * BX + threadIdx.x;
   for (int i = tid; i < (BY + 5) * (BX + 5); i += BX * BY) {
     int ty = i / (BX + 5), tx = i - ty * (BX + 5);
@@ -38,59 +64,75 @@ __global__ void __launch_bounds__(BX* BY)
       v = (float)mm[(size_t)gy * W + gx] * scale;
     else
       v = fin[(size_t)gy * W + gx];
-    tex[ty][tx] = v;
+    m.tex[ty][tx] = v;
   }
   __syncthreads();
   for (int i = tid; i < (BY + 4) * (BX + 4); i += BX * BY) {
     int ty = i / (BX + 4), tx = i - ty * (BX + 4);
-    tap[ty][tx] = 0.25f * ((tex[ty][tx] + tex[ty][tx + 1]) + (tex[ty + 1][tx] + tex[ty + 1][tx + 1]));
+    m.tap[ty][tx] = 0.25f * ((m.tex[ty][tx] + m.tex[ty][tx + 1]) + (m.tex[ty + 1][tx] + m.tex[ty + 1][tx + 1]));
   }
   __syncthreads();
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = x0 + tx, y = y0 + ty;
-  if (x >= W || y >= H) return;
-  if (FROM_MM) raw_out[(size_t)y * W + x] = tex[ty + 3][tx + 3];
-  const float g[5] = {g0, g1, g2, g1, g0};
-  const float denom = 2.0f * 0.1f * 0.1f;  // 2 sigma_r^2, sigma_r = 0.1 m (z_yooji_cuda_img_proc.cu:44,91)
-  const float center = tap[ty + 2][tx + 2];
-  float t = 0.0f, sum = 0.0f;
-#pragma unroll
-  for (int i = -2; i <= 2; i++) {
-#pragma unroll
-    for (int j = -2; j <= 2; j++) {
-      float cur = tap[ty + 2 + i][tx + 2 + j];
-      if (cur <= 0.0f) {
-        out[(size_t)y * W + x] = 0.0f;
-        return;
-      }
-      float mod = (center - cur) * (center - cur);
-      float factor = g[i + 2] * g[j + 2] * __expf(-mod / denom);
-      t += factor * cur;
-      sum += factor;
-    }
+  if (x < W && y < H) {
+    if (FROM_MM) raw_out[(size_t)y * W + x] = m.tex[ty + 3][tx + 3];
+    out[(size_t)y * W + x] = bilateral_px(m, tx, ty, g);
   }
-  out[(size_t)y * W + x] = t / sum;
+}
+
+__global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __restrict__ bt) {
+  __shared__ BilateralSmem m;
+  const int n = bt->n;
+  const int total = bt->bil[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int t;
+    const int slot = find_slot(bt->bil, n, item, t);
+    const SessionDev* __restrict__ s = bt->s[slot];
+    const int W = s->lv[0].W, H = s->lv[0].H;
+    const int tw = (W + BX - 1) / BX;
+    const float g[5] = {s->gauss[0], s->gauss[1], s->gauss[2], s->gauss[1], s->gauss[0]};
+    bilateral_tile<true>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
+                         (t / tw) * BY, g);
+    __syncthreads();  // the next tile overwrites the shared tiles
+  }
+}
+
+__global__ void __launch_bounds__(BX* BY)
+    k_bilateral_float(const float* __restrict__ in, float* __restrict__ out, int W, int H, float g0, float g1,
+                      float g2) {
+  __shared__ BilateralSmem m;
+  const float g[5] = {g0, g1, g2, g1, g0};
+  bilateral_tile<false>(m, nullptr, in, 1.0f, nullptr, out, W, H, blockIdx.x * BX, blockIdx.y * BY, g);
 }
 
 // level l -> l+1: separable [1 4 6 4 1] smoothing (borders 0, no validity
 // mask) evaluated only at the kept pixel (2 i2 + 1, 2 j2 + 1)
-__global__ void k_pyramid_down(const float* __restrict__ in, int w, int h, float* __restrict__ out,
-                               int w2, int h2) {
-  int i2 = blockIdx.x * blockDim.x + threadIdx.x;
-  int j2 = blockIdx.y * blockDim.y + threadIdx.y;
-  if (i2 >= w2 || j2 >= h2) return;
-  int i = 2 * i2 + 1, j = 2 * j2 + 1;
-  float v = 0.0f;
-  if (i >= 2 && i < w - 2 && j >= 2 && j < h - 2) {
-    float pad[5];
+__global__ void __launch_bounds__(256) k_pyramid_batch(const BatchTable* __restrict__ bt, int l2) {
+  const int n = bt->n;
+  const int* pre = bt->pyr[l2 - 1];
+  const int total = pre[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int t;
+    const int slot = find_slot(pre, n, item, t);
+    const SessionDev* __restrict__ s = bt->s[slot];
+    const int w = s->lv[l2 - 1].W, h = s->lv[l2 - 1].H, w2 = s->lv[l2].W, h2 = s->lv[l2].H;
+    const int tw = (w2 + 31) / 32;
+    const int i2 = (t % tw) * 32 + threadIdx.x, j2 = (t / tw) * 8 + threadIdx.y;
+    if (i2 >= w2 || j2 >= h2) continue;
+    const float* __restrict__ in = s->depth[l2 - 1];
+    int i = 2 * i2 + 1, j = 2 * j2 + 1;
+    float v = 0.0f;
+    if (i >= 2 && i < w - 2 && j >= 2 && j < h - 2) {
+      float pad[5];
 #pragma unroll
-    for (int r = 0; r < 5; r++) {
-      const float* p = in + (size_t)(j - 2 + r) * w;
-      pad[r] = p[i - 2] + p[i + 2] + 4.0f * p[i - 1] + 4.0f * p[i + 1] + 6.0f * p[i];
+      for (int r = 0; r < 5; r++) {
+        const float* p = in + (size_t)(j - 2 + r) * w;
+        pad[r] = p[i - 2] + p[i + 2] + 4.0f * p[i - 1] + 4.0f * p[i + 1] + 6.0f * p[i];
+      }
+      v = (pad[0] + pad[4] + 4.0f * pad[1] + 4.0f * pad[3] + 6.0f * pad[2]) / (16.0f * 16.0f);
     }
-    v = (pad[0] + pad[4] + 4.0f * pad[1] + 4.0f * pad[3] + 6.0f * pad[2]) / (16.0f * 16.0f);
+    s->depth[l2][(size_t)j2 * w2 + i2] = v;
   }
-  out[(size_t)j2 * w2 + i2] = v;
 }
 
 // ---------------------------------------------------------------------------
@@ -108,23 +150,18 @@ __global__ void k_pyramid_down(const float* __restrict__ in, int w, int h, float
 //   a wavefront across the lanes of the warp.
 // pass 3 (parallel): vertex valid = depth > 0 and not rejected; normal valid =
 //   code 1 and neither the left nor the upper neighbour rejected.
+// A session's items cover its levels in order; the per-level tile counts
+// follow from the level sizes.
 // ---------------------------------------------------------------------------
-struct LevelPtrs {
-  const float* depth;
-  float4* vtx;
-  float4* nrm;
-  uint8_t* code;
-  uint32_t* amask;
-  uint32_t* rmask;
-  int w, h;
-  float K[4];
-};
-struct InmapArgs {
-  LevelPtrs lv[kMaxLevels];
-  int levels;
-  int tiles[kMaxLevels + 1];  // prefix of tiles per level (32x8 for pre, 16x16 for post)
-  int tiles_pre[kMaxLevels + 1];
-};
+__device__ inline int level_of_tile(const SessionDev& s, int tile_w, int tile_h, int& t) {
+  int l = 0;
+  for (; l < s.levels - 1; l++) {
+    const int nt = ((s.lv[l].W + tile_w - 1) / tile_w) * ((s.lv[l].H + tile_h - 1) / tile_h);
+    if (t < nt) break;
+    t -= nt;
+  }
+  return l;
+}
 
 __device__ inline bool bp_valid(const float* depth, int w, int x, int y, const float* K, F3& p) {
   float d = depth[(size_t)y * w + x];
@@ -133,63 +170,64 @@ __device__ inline bool bp_valid(const float* depth, int w, int x, int y, const f
   return true;
 }
 
-__global__ void __launch_bounds__(256) k_inmap_pre(InmapArgs a) {
-  int b = blockIdx.x, l = 0;
-  while (l + 1 < a.levels && b >= a.tiles_pre[l + 1]) l++;
-  const LevelPtrs& L = a.lv[l];
-  const int t = b - a.tiles_pre[l];
-  const int tw = (L.w + 31) / 32;
-  const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * 8 + threadIdx.y;
-  if (y >= L.h) return;  // whole warp (a warp is one 32-pixel row segment)
-  uint8_t code = 0;
-  float4 n = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
-  if (x >= 1 && x < L.w - 1 && y >= 1 && y < L.h - 1) {
-    F3 c, x1, x2, y1, y2;
-    bool ok = bp_valid(L.depth, L.w, x, y, L.K, c) && bp_valid(L.depth, L.w, x - 1, y, L.K, x1) &&
-              bp_valid(L.depth, L.w, x + 1, y, L.K, x2) && bp_valid(L.depth, L.w, x, y - 1, L.K, y1) &&
-              bp_valid(L.depth, L.w, x, y + 1, L.K, y2);
-    if (ok) {
-      float dx = x2.x - x1.x;
-      float dy = y2.y - y1.y;
-      if (!(fabsf(dx) < 1.0e-7f) && !(fabsf(dy) < 1.0e-7f)) {
-        float dzdx = (x2.z - x1.z) / dx;
-        float dzdy = (y2.z - y1.z) / dy;
-        float len = sqrtf(dzdx * dzdx + dzdy * dzdy + 1.0f);
-        float nx = dzdx / len, ny = dzdy / len, nz = -1.0f / len;
-        // -n_z < cos(60 deg), the threshold taken in double as the reference's cos()
-        if (-(double)nz < 0.50000000000000011) {
-          code = 2;
-        } else {
-          code = 1;
-          n = make_float4(nx, ny, nz, 0.0f);
+__global__ void __launch_bounds__(256) k_inmap_pre(const BatchTable* __restrict__ bt) {
+  const int n = bt->n;
+  const int total = bt->ipre[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int t;
+    const int slot = find_slot(bt->ipre, n, item, t);
+    const SessionDev& s = *bt->s[slot];
+    const int l = level_of_tile(s, 32, 8, t);
+    const int w = s.lv[l].W, h = s.lv[l].H;
+    const float K[4] = {s.lv[l].K[0], s.lv[l].K[1], s.lv[l].K[2], s.lv[l].K[3]};
+    const float* __restrict__ depth = s.depth[l];
+    const int tw = (w + 31) / 32;
+    const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * 8 + threadIdx.y;
+    if (y >= h) continue;  // whole warp (a warp is one 32-pixel row segment)
+    uint8_t code = 0;
+    float4 nv = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
+    if (x >= 1 && x < w - 1 && y >= 1 && y < h - 1) {
+      F3 c, x1, x2, y1, y2;
+      bool ok = bp_valid(depth, w, x, y, K, c) && bp_valid(depth, w, x - 1, y, K, x1) &&
+                bp_valid(depth, w, x + 1, y, K, x2) && bp_valid(depth, w, x, y - 1, K, y1) &&
+                bp_valid(depth, w, x, y + 1, K, y2);
+      if (ok) {
+        float dx = x2.x - x1.x;
+        float dy = y2.y - y1.y;
+        if (!(fabsf(dx) < 1.0e-7f) && !(fabsf(dy) < 1.0e-7f)) {
+          float dzdx = (x2.z - x1.z) / dx;
+          float dzdy = (y2.z - y1.z) / dy;
+          float len = sqrtf(dzdx * dzdx + dzdy * dzdy + 1.0f);
+          float nx = dzdx / len, ny = dzdy / len, nz = -1.0f / len;
+          // -n_z < cos(60 deg), the threshold taken in double as the reference's cos()
+          if (-(double)nz < 0.50000000000000011) {
+            code = 2;
+          } else {
+            code = 1;
+            nv = make_float4(nx, ny, nz, 0.0f);
+          }
         }
       }
     }
+    const unsigned m = __ballot_sync(0xffffffffu, code == 2);
+    if (threadIdx.x == 0) s.in_amask[l][(size_t)y * tw + (t % tw)] = m;
+    if (x >= w) continue;
+    s.in_code[l][(size_t)y * w + x] = code;
+    s.in_nrm[l][(size_t)y * w + x] = nv;
   }
-  const unsigned m = __ballot_sync(0xffffffffu, code == 2);
-  if (threadIdx.x == 0) L.amask[(size_t)y * tw + (t % tw)] = m;
-  if (x >= L.w) return;
-  L.code[(size_t)y * L.w + x] = code;
-  L.nrm[(size_t)y * L.w + x] = n;
 }
 
-// one block per level: the block stages the level's code-2 bitmasks in
-// shared memory, then warp 0 sweeps the rows as a wavefront: at step t lane l
-// solves row t - l for its words, taking the carry of the row's earlier words
-// from lane l - 1 (computed at step t - 1) and the rejections of the row above
-// from its own registers, so one step costs one shuffle.
-__global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
-  extern __shared__ uint32_t amask[];  // [h][nw]
-  const LevelPtrs& L = a.lv[blockIdx.x];
-  const int nw = (L.w + 31) >> 5;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int nwords = L.h * nw;
-  for (int i = threadIdx.x; i < nwords; i += blockDim.x) amask[i] = L.amask[i];
-  __syncthreads();
-  if (warp != 0) return;
+// Row sweep of one level: warp 0 sweeps the rows as a wavefront: at step t
+// lane l solves row t - l for its words, taking the carry of the row's earlier
+// words from lane l - 1 (computed at step t - 1) and the rejections of the row
+// above from its own registers, so one step costs one shuffle.  am: the
+// level's code-2 bitmasks (shared memory when they fit, else global).
+__device__ void scan_level(const uint32_t* am, uint32_t* __restrict__ rmask, int w, int h) {
+  const int nw = (w + 31) >> 5;
+  const int lane = threadIdx.x & 31;
   const uint32_t M0 = 0x55555555u, M1 = 0xaaaaaaaau;
   const int wpl = (nw + 31) >> 5;  // words per lane (1 up to 1024 pixels, 2 up to 2048)
-  const int steps = L.h + 31;
+  const int steps = h + 31;
   if (wpl == 1) {
     // both outcomes of a word are formed before its carry arrives, so a step's
     // critical path is one shuffle and one select
@@ -197,10 +235,10 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
     uint32_t rup = 0u, cout = 0u;
     for (int t = 0; t < steps; t++) {
       const int row = t - lane;
-      const bool valid = act && row >= 0 && row < L.h;
+      const bool valid = act && row >= 0 && row < h;
       uint32_t R0 = 0u, R1 = 0u;
       if (valid && row > 0) {  // row 0 is never processed (interior rows only)
-        const uint32_t C = amask[row * nw + lane] & ~rup;
+        const uint32_t C = am[row * nw + lane] & ~rup;
         const uint32_t st = C & ~(C << 1);  // run starts (bit 0 counted as a start)
         const uint32_t ev = (C & ((C + ((st & ~1u) & M0)) ^ C)) & M0;
         const uint32_t od = (C & ((C + ((st & ~1u) & M1)) ^ C)) & M1;
@@ -214,7 +252,7 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
       if (lane == 0) cin = 0u;
       const uint32_t R = cin ? R1 : R0;
       if (valid) {
-        L.rmask[(size_t)row * nw + lane] = R;
+        rmask[(size_t)row * nw + lane] = R;
         rup = R;
       }
       cout = valid ? (R >> 31) : 0u;
@@ -228,21 +266,21 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
     if (lane == 0) cin = 0u;
     const int row = t - lane;
     uint32_t cout = 0u;
-    if (row >= 0 && row < L.h) {
+    if (row >= 0 && row < h) {
 #pragma unroll
       for (int q = 0; q < 2; q++) {
         const int wi = lane * wpl + q;
         if (q < wpl && wi < nw) {
           uint32_t R = 0u;
           if (row > 0) {
-            const uint32_t C = amask[row * nw + wi] & ~rup[q];
+            const uint32_t C = am[row * nw + wi] & ~rup[q];
             const uint32_t st = C & ~(C << 1);
             const uint32_t rest = st & ~1u;
             const uint32_t se = (rest & M0) | (cin ? 0u : (st & 1u));
             const uint32_t so = (rest & M1) | (cin ? (st & 1u) : 0u);
             R = ((C & ((C + se) ^ C)) & M0) | ((C & ((C + so) ^ C)) & M1);
           }
-          L.rmask[(size_t)row * nw + wi] = R;
+          rmask[(size_t)row * nw + wi] = R;
           rup[q] = R;
           cin = R >> 31;
         }
@@ -253,103 +291,117 @@ __global__ void __launch_bounds__(1024) k_inmap_scan(InmapArgs a) {
   }
 }
 
-__global__ void k_inmap_post(InmapArgs a) {
-  int b = blockIdx.x, l = 0;
-  while (l + 1 < a.levels && b >= a.tiles[l + 1]) l++;
-  const LevelPtrs& L = a.lv[l];
-  int t = b - a.tiles[l];
-  int tw = (L.w + 15) / 16;
-  int x = (t % tw) * 16 + threadIdx.x, y = (t / tw) * 16 + threadIdx.y;
-  if (x >= L.w || y >= L.h) return;
-  const int nw = (L.w + 31) >> 5;
-  auto rej = [&](int xx, int yy) -> bool {
-    if (xx < 0 || yy < 0) return false;
-    return (L.rmask[(size_t)yy * nw + (xx >> 5)] >> (xx & 31)) & 1u;
-  };
-  size_t idx = (size_t)y * L.w + x;
-  float d = L.depth[idx];
-  float4 v = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
-  if (d > 0.0f && !rej(x, y)) {
-    F3 p = back_project((float)x, (float)y, L.K, d);
-    v = make_float4(p.x, p.y, p.z, 1.0f);
+// one block per (session, level) item
+__global__ void __launch_bounds__(1024) k_inmap_scan(const BatchTable* __restrict__ bt) {
+  extern __shared__ uint32_t amask[];  // [h][nw] of the current item
+  const int n = bt->n;
+  const int total = bt->scan[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int l;
+    const int slot = find_slot(bt->scan, n, item, l);
+    const SessionDev& s = *bt->s[slot];
+    const int w = s.lv[l].W, h = s.lv[l].H;
+    const int nwords = h * ((w + 31) >> 5);
+    const uint32_t* src = s.in_amask[l];
+    const bool staged = nwords * 4 <= kScanSmem;
+    if (staged)
+      for (int i = threadIdx.x; i < nwords; i += blockDim.x) amask[i] = src[i];
+    __syncthreads();
+    if (threadIdx.x < 32) scan_level(staged ? amask : src, s.in_rmask[l], w, h);
+    __syncthreads();  // the next item restages the shared masks
   }
-  L.vtx[idx] = v;
-  uint8_t code = L.code[idx];
-  float4 n = L.nrm[idx];
-  if (code == 1 && !rej(x - 1, y) && !rej(x, y - 1)) {
-    n.w = 1.0f;
-  } else {
-    n = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
-  }
-  L.nrm[idx] = n;
 }
 
-InmapArgs make_inmap_args(const SessionDev& h) {
-  InmapArgs a;
-  a.levels = h.levels;
-  a.tiles[0] = 0;
-  a.tiles_pre[0] = 0;
-  for (int l = 0; l < kMaxLevels; l++) {
-    LevelPtrs& L = a.lv[l];
-    L.depth = h.depth[l];
-    L.vtx = h.in_vtx[l];
-    L.nrm = h.in_nrm[l];
-    L.code = h.in_code[l];
-    L.amask = h.in_amask[l];
-    L.rmask = h.in_rmask[l];
-    L.w = h.lv[l].W;
-    L.h = h.lv[l].H;
-    for (int k = 0; k < 4; k++) L.K[k] = h.lv[l].K[k];
-    int nt = (l < h.levels) ? ((L.w + 15) / 16) * ((L.h + 15) / 16) : 0;
-    a.tiles[l + 1] = a.tiles[l] + nt;
-    int np = (l < h.levels) ? ((L.w + 31) / 32) * ((L.h + 7) / 8) : 0;
-    a.tiles_pre[l + 1] = a.tiles_pre[l] + np;
+__global__ void __launch_bounds__(256) k_inmap_post(const BatchTable* __restrict__ bt) {
+  const int n = bt->n;
+  const int total = bt->ipost[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int t;
+    const int slot = find_slot(bt->ipost, n, item, t);
+    const SessionDev& s = *bt->s[slot];
+    const int l = level_of_tile(s, 16, 16, t);
+    const int w = s.lv[l].W, h = s.lv[l].H;
+    const int tw = (w + 15) / 16;
+    const int x = (t % tw) * 16 + threadIdx.x, y = (t / tw) * 16 + threadIdx.y;
+    if (x >= w || y >= h) continue;
+    const int nw = (w + 31) >> 5;
+    const uint32_t* __restrict__ rm = s.in_rmask[l];
+    auto rej = [&](int xx, int yy) -> bool {
+      if (xx < 0 || yy < 0) return false;
+      return (rm[(size_t)yy * nw + (xx >> 5)] >> (xx & 31)) & 1u;
+    };
+    const size_t idx = (size_t)y * w + x;
+    const float d = s.depth[l][idx];
+    float4 v = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
+    if (d > 0.0f && !rej(x, y)) {
+      F3 p = back_project((float)x, (float)y, s.lv[l].K, d);
+      v = make_float4(p.x, p.y, p.z, 1.0f);
+    }
+    s.in_vtx[l][idx] = v;
+    const uint8_t code = s.in_code[l][idx];
+    float4 nv = s.in_nrm[l][idx];
+    if (code == 1 && !rej(x - 1, y) && !rej(x, y - 1)) {
+      nv.w = 1.0f;
+    } else {
+      nv = make_float4(-100.0f, -100.0f, -100.0f, 0.0f);
+    }
+    s.in_nrm[l][idx] = nv;
   }
-  return a;
 }
 
 }  // namespace
 
-void launch_filter(const SessionDev* /*d*/, const SessionDev& h, cudaStream_t st) {
+void launch_filter(const BatchTable* bt, cudaStream_t st) {
+  const int grid = sm_count() * 8;
+  k_bilateral_batch<<<grid, dim3(BX, BY), 0, st>>>(bt);
+  for (int l = 1; l < kMaxLevels; l++) k_pyramid_batch<<<grid, dim3(32, 8), 0, st>>>(bt, l);
+}
+
+void launch_input_maps(const BatchTable* bt, cudaStream_t st) {
+  const int grid = sm_count() * 8;
+  k_inmap_pre<<<grid, dim3(32, 8), 0, st>>>(bt);
+  k_inmap_scan<<<kMaxSlots * kMaxLevels, 1024, kScanSmem, st>>>(bt);
+  k_inmap_post<<<grid, dim3(16, 16), 0, st>>>(bt);
+}
+
+void launch_bilateral_float(const SessionDev& h, const float* in, float* out, cudaStream_t st) {
   const int W = h.lv[0].W, H = h.lv[0].H;
   dim3 blk(BX, BY), grd((W + BX - 1) / BX, (H + BY - 1) / BY);
-  k_bilateral<true><<<grd, blk, 0, st>>>(h.depth_mm, nullptr, h.depth_scale, h.depth_raw, h.depth[0],
-                                         W, H, h.gauss[0], h.gauss[1], h.gauss[2]);
-  for (int l = 1; l < h.levels; l++) {
-    dim3 b2(32, 8), g2((h.lv[l].W + 31) / 32, (h.lv[l].H + 7) / 8);
-    k_pyramid_down<<<g2, b2, 0, st>>>(h.depth[l - 1], h.lv[l - 1].W, h.lv[l - 1].H, h.depth[l],
-                                      h.lv[l].W, h.lv[l].H);
-  }
-}
-
-void launch_bilateral_float(const SessionDev* /*d*/, const SessionDev& h, const float* in, float* out,
-                            cudaStream_t st) {
-  const int W = h.lv[0].W, H = h.lv[0].H;
-  dim3 blk(BX, BY), grd((W + BX - 1) / BX, (H + BY - 1) / BY);
-  k_bilateral<false><<<grd, blk, 0, st>>>(nullptr, in, 1.0f, nullptr, out, W, H, h.gauss[0], h.gauss[1],
-                                          h.gauss[2]);
-}
-
-size_t inmap_scan_smem(const SessionDev& h) {
-  size_t m = 0;
-  for (int l = 0; l < h.levels; l++) {
-    size_t b = (size_t)h.lv[l].H * ((h.lv[l].W + 31) / 32) * 4;
-    if (b > m) m = b;
-  }
-  return m;
-}
-
-void launch_input_maps(const SessionDev* /*d*/, const SessionDev& h, cudaStream_t st) {
-  InmapArgs a = make_inmap_args(h);
-  dim3 b16(16, 16);
-  k_inmap_pre<<<a.tiles_pre[h.levels], dim3(32, 8), 0, st>>>(a);
-  size_t smem = inmap_scan_smem(h);
-  k_inmap_scan<<<h.levels, 1024, smem, st>>>(a);
-  k_inmap_post<<<a.tiles[h.levels], b16, 0, st>>>(a);
+  k_bilateral_float<<<grd, blk, 0, st>>>(in, out, W, H, h.gauss[0], h.gauss[1], h.gauss[2]);
 }
 
 void configure_filter_kernels() {
-  cudaFuncSetAttribute(k_inmap_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(k_inmap_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, kScanSmem);
+}
+
+// work-item prefixes of a batch; host_recs are the host copies of the
+// session records, dev_recs their device addresses
+void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs,
+                      int n) {
+  std::memset(&hb, 0, sizeof(hb));
+  hb.n = n;
+  for (int i = 0; i < n; i++) {
+    const SessionDev& h = *host_recs[i];
+    hb.s[i] = dev_recs[i];
+    const bool nm = h.cos_normal > -2.0f;
+    int ipre = 0, ipost = 0, ray = 0;
+    for (int l = 0; l < h.levels; l++) {
+      const int w = h.lv[l].W, hh = h.lv[l].H;
+      ipre += ((w + 31) / 32) * ((hh + 7) / 8);
+      ipost += ((w + 15) / 16) * ((hh + 15) / 16);
+      ray += ((w + 15) / 16) * ((hh + 7) / 8);
+    }
+    hb.bil[i + 1] = hb.bil[i] + ((h.lv[0].W + BX - 1) / BX) * ((h.lv[0].H + BY - 1) / BY);
+    for (int l = 1; l < kMaxLevels; l++)
+      hb.pyr[l - 1][i + 1] =
+          hb.pyr[l - 1][i] + (l < h.levels ? ((h.lv[l].W + 31) / 32) * ((h.lv[l].H + 7) / 8) : 0);
+    hb.ipre[i + 1] = hb.ipre[i] + (nm ? ipre : 0);
+    hb.ipost[i + 1] = hb.ipost[i] + (nm ? ipost : 0);
+    hb.scan[i + 1] = hb.scan[i] + (nm ? h.levels : 0);
+    for (int l = 0; l < kMaxLevels; l++)
+      hb.icp[l][i + 1] = hb.icp[l][i] + (l < h.levels ? icp_blocks(h.lv[l].W * h.lv[l].H) : 0);
+    hb.ray[i + 1] = hb.ray[i] + ray;
+  }
 }
 
 }  // namespace vs

@@ -19,6 +19,14 @@
 // Convergence and failure are flags in device memory that the following
 // launches read first, so a whole frame of iterations is one CUDA graph with
 // no host round trip.  Nothing in these kernels waits on another block.
+//
+// Batches: one launch per iteration serves every session of a batch table.
+// A session at level l owns icp_blocks(W_l H_l) block ranges ("virtual
+// blocks"), laid out as they would be in a grid of that size; the persistent
+// grid walks the ranges of all sessions, each session has its own partial
+// buffer and arrival counter, and the range that arrives last for a session
+// reduces and solves that session's system.  Sums therefore run in the same
+// order whatever else shares the launch.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -370,107 +378,33 @@ __device__ void rigid_inverse(const double* T, double* I) {
   I[15] = 1.0;
 }
 
-__global__ void k_icp_begin(SessionDev* s, int allow_skip, int with_init, const float* init) {
-  Pose* P = s->pose;
+__global__ void k_icp_begin(const BatchTable* __restrict__ bt, int allow_skip, int with_init,
+                            const float* init) {
+  const int i = threadIdx.x;
+  if (i >= bt->n) return;
+  Pose* P = bt->s[i]->pose;
   P->skip = (allow_skip && P->frame == 0) ? 1 : 0;
   P->failed = 0;
   P->iters_run = 0;
   P->valid_count = 0;
   for (int l = 0; l < kMaxLevels; l++) P->level_done[l] = (with_init && l > 0) ? 1 : 0;
   double T[16];
-  for (int i = 0; i < 16; i++) T[i] = (i % 5 == 0) ? 1.0 : 0.0;
+  for (int k = 0; k < 16; k++) T[k] = (k % 5 == 0) ? 1.0 : 0.0;
   if (with_init && init)
-    for (int i = 0; i < 16; i++) T[i] = (double)init[i];
+    for (int k = 0; k < 16; k++) T[k] = (double)init[k];
   double I[16];
   rigid_inverse(T, I);
-  for (int i = 0; i < 16; i++) {
-    P->T12[i] = T[i];
-    P->T21[i] = (float)I[i];
+  for (int k = 0; k < 16; k++) {
+    P->T12[k] = T[k];
+    P->T21[k] = (float)I[k];
   }
 }
 
-template <int MODE>
-__global__ void __launch_bounds__(kThreads, 3) k_icp_iter(const SessionDev* __restrict__ s, int level) {
-  Pose* P = s->pose;
-  if (P->skip | P->failed | P->level_done[level]) return;  // uniform across the grid
-  const int w = s->lv[level].W, h = s->lv[level].H;
-  float K[4], T21[12];
-#pragma unroll
-  for (int k = 0; k < 4; k++) K[k] = s->lv[level].K[k];
-#pragma unroll
-  for (int k = 0; k < 12; k++) T21[k] = P->T21[k];
-  const float th = s->th_icp, cosn = s->cos_normal;
-  const float* depth = s->depth[level];
-  const float4* mvtx = s->m_vtx[level];
-  const float4* mnrm = s->m_nrm[level];
-  const float4* innrm = s->in_nrm[level];
-
-  Acc<MODE> acc;
-  acc.zero();
-  const int npix = w * h;
-  for (int p = blockIdx.x * kThreads + threadIdx.x; p < npix; p += gridDim.x * kThreads) {
-    int y = p / w, x = p - y * w;
-    float A[6], b;
-    if (!icp_term(x, y, w, h, K, depth, mvtx, mnrm, innrm, T21, th, cosn, A, b)) continue;
-#pragma unroll
-    for (int i = 0; i < 6; i++)
-#pragma unroll
-      for (int j = i; j < 6; j++) acc.add(tri_index(i, j), A[i] * A[j]);
-#pragma unroll
-    for (int i = 0; i < 6; i++) acc.add(21 + i, A[i] * b);
-    acc.add(27, 1.0f);
-    acc.add(28, b * b);
-  }
-  acc.begin_tree();
-#pragma unroll
-  for (int m = 16; m >= 1; m >>= 1) acc.shfl_add(m);
-
-  typedef typename PartT<MODE>::type PT;
-  __shared__ PT wsum[kThreads / 32][29];
-  __shared__ int s_last;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (lane == 0)
-#pragma unroll
-    for (int k = 0; k < 29; k++) wsum[warp][k] = acc.get(k);
-  __syncthreads();
-  PT* part = reinterpret_cast<PT*>(s->partials) + (size_t)blockIdx.x * kPartials;
-  if (threadIdx.x < 29) {
-    PT v = wsum[0][threadIdx.x];
-    for (int q = 1; q < kThreads / 32; q++) v = combine(v, wsum[q][threadIdx.x], MODE);
-    part[threadIdx.x] = v;
-    __threadfence();
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    unsigned t = atomicAdd(s->icp_counter, 1u);
-    s_last = (t == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (!s_last) return;
-
-  // ---- last block: deterministic grid sum, then the solve ----
-  __threadfence();
-  __shared__ double fin[29];
-  {
-    // 8 threads per quantity, each a fixed stride over blocks, then a fixed
-    // shuffle tree
-    const int k = threadIdx.x >> 3, j = threadIdx.x & 7;
-    PT v;
-    v.x = 0;
-    v.y = 0;
-    if (k < 29) {
-      const PT* base = reinterpret_cast<const PT*>(s->partials);
-      for (int bb = j; bb < (int)gridDim.x; bb += 8) v = combine(v, __ldcg(base + (size_t)bb * kPartials + k), MODE);
-    }
-#pragma unroll
-    for (int m = 4; m >= 1; m >>= 1) v = combine(v, shfl_xor2(v, m), MODE);
-    if (k < 29 && j == 0) fin[k] = (double)v.x + (double)v.y;
-  }
-  __syncthreads();
-  if (threadIdx.x >= 32) return;
-  // ---- warp 0: FP64 solve and SE(3) update, lane-parallel ----
+// warp 0 of the block that closed a session's iteration: FP64 solve and SE(3)
+// update, lane-parallel (kept out of line so the pixel loop's register
+// allocation does not carry it)
+__device__ __noinline__ void icp_solve_update(Pose* P, const double* fin, int level) {
   const int ln = threadIdx.x;
-  if (ln == 0) *s->icp_counter = 0u;
   if (ln < 29) P->last_sums[ln] = fin[ln];
   if (ln == 0) {
     P->iters_run += 1;
@@ -495,10 +429,132 @@ __global__ void __launch_bounds__(kThreads, 3) k_icp_iter(const SessionDev* __re
   if (ln < 16) E[ln] = e;
   __syncwarp();
   warp_compose_and_invert(E, P->T12, Tn, ln, P->T12, P->T21);
+  __syncwarp();
 }
 
-__global__ void k_icp_finish(SessionDev* s, int frame_mode) {
-  Pose* P = s->pose;
+// Blocks take ranges from an atomic counter: a block that closes a session
+// (reduction + solve, ~10 us) simply takes no new range meanwhile, so the
+// closing work of different sessions overlaps instead of queueing behind a
+// static assignment.  The last block to leave clears the counters.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads, 3)
+    k_icp_iter(const BatchTable* __restrict__ bt, unsigned* __restrict__ work, int level, int iter) {
+  typedef typename PartT<MODE>::type PT;
+  __shared__ PT wsum[kThreads / 32][29];
+  __shared__ int s_last, s_item;
+  __shared__ double fin[29];
+  __shared__ float sT21[12], sK[4];
+  const int n = bt->n;
+  const int* pre = bt->icp[level];
+  const int total = pre[n];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(work, 1u);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= total) break;
+    int vb;
+    const int slot = find_slot(pre, n, item, vb);
+    const SessionDev* __restrict__ s = bt->s[slot];
+    Pose* P = s->pose;
+    // uniform across the session's ranges: no range of this session has
+    // closed the iteration yet when any of them reads the flags
+    if (iter >= s->iters[level] || (P->skip | P->failed | P->level_done[level])) {
+      __syncthreads();  // every thread has read s_item before the next fetch
+      continue;
+    }
+    const int nvb = pre[slot + 1] - pre[slot];
+    const int w = s->lv[level].W, h = s->lv[level].H;
+    // the pose and intrinsics are read from shared memory in the pixel loop,
+    // which leaves the registers to the 29 running sums
+    if (threadIdx.x < 12) sT21[threadIdx.x] = P->T21[threadIdx.x];
+    if (threadIdx.x < 4) sK[threadIdx.x] = s->lv[level].K[threadIdx.x];
+    __syncthreads();
+    const float* K = sK;
+    const float* T21 = sT21;
+    const float th = s->th_icp, cosn = s->cos_normal;
+    const float* depth = s->depth[level];
+    const float4* mvtx = s->m_vtx[level];
+    const float4* mnrm = s->m_nrm[level];
+    const float4* innrm = s->in_nrm[level];
+
+    Acc<MODE> acc;
+    acc.zero();
+    const int npix = w * h;
+    for (int p = vb * kThreads + threadIdx.x; p < npix; p += nvb * kThreads) {
+      int y = p / w, x = p - y * w;
+      float A[6], b;
+      if (!icp_term(x, y, w, h, K, depth, mvtx, mnrm, innrm, T21, th, cosn, A, b)) continue;
+#pragma unroll
+      for (int i = 0; i < 6; i++)
+#pragma unroll
+        for (int j = i; j < 6; j++) acc.add(tri_index(i, j), A[i] * A[j]);
+#pragma unroll
+      for (int i = 0; i < 6; i++) acc.add(21 + i, A[i] * b);
+      acc.add(27, 1.0f);
+      acc.add(28, b * b);
+    }
+    acc.begin_tree();
+#pragma unroll
+    for (int m = 16; m >= 1; m >>= 1) acc.shfl_add(m);
+
+    if (lane == 0)
+#pragma unroll
+      for (int k = 0; k < 29; k++) wsum[warp][k] = acc.get(k);
+    __syncthreads();
+    PT* part = reinterpret_cast<PT*>(s->partials) + (size_t)vb * kPartials;
+    if (threadIdx.x < 29) {
+      PT v = wsum[0][threadIdx.x];
+      for (int q = 1; q < kThreads / 32; q++) v = combine(v, wsum[q][threadIdx.x], MODE);
+      part[threadIdx.x] = v;
+      __threadfence();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned t = atomicAdd(s->icp_counter, 1u);
+      s_last = (t == (unsigned)nvb - 1u);
+    }
+    __syncthreads();
+    if (s_last) {
+      // ---- last range of this session: deterministic sum, then the solve ----
+      __threadfence();
+      {
+        // 8 threads per quantity, each a fixed stride over the ranges, then a
+        // fixed shuffle tree
+        const int k = threadIdx.x >> 3, j = threadIdx.x & 7;
+        PT v;
+        v.x = 0;
+        v.y = 0;
+        if (k < 29) {
+          const PT* base = reinterpret_cast<const PT*>(s->partials);
+          for (int bb = j; bb < nvb; bb += 8) v = combine(v, __ldcg(base + (size_t)bb * kPartials + k), MODE);
+        }
+#pragma unroll
+        for (int m = 4; m >= 1; m >>= 1) v = combine(v, shfl_xor2(v, m), MODE);
+        if (k < 29 && j == 0) fin[k] = (double)v.x + (double)v.y;
+      }
+      __syncthreads();
+      if (threadIdx.x < 32) {
+        if (threadIdx.x == 0) *s->icp_counter = 0u;
+        icp_solve_update(P, fin, level);
+      }
+    }
+    __syncthreads();  // shared sums and s_item are reused by the next range
+  }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(work + 1, 1u) == gridDim.x - 1) {
+      work[0] = 0u;
+      work[1] = 0u;
+      __threadfence();
+    }
+  }
+}
+
+// one warp per slot
+__global__ void k_icp_finish(const BatchTable* __restrict__ bt, int frame_mode) {
+  if ((int)blockIdx.x >= bt->n) return;
+  Pose* P = bt->s[blockIdx.x]->pose;
   const int ln = threadIdx.x;
   __shared__ double Tn[16], A[16];
   if (!P->skip && !P->failed) {
@@ -536,6 +592,22 @@ __global__ void k_pose_set(SessionDev* s, const double* T) {
   if (ln == 3 || ln == 7 || ln == 11) P->center[ln >> 2] = (float)Ti;
 }
 
+// the 80-byte pose heads (float pose, tracked, iterations, count, frame) of
+// every slot, packed slot after slot for one device-to-host copy
+__global__ void k_gather_heads(const BatchTable* __restrict__ bt, uint32_t* __restrict__ out) {
+  const int slot = blockIdx.x;
+  if (slot >= bt->n) return;
+  constexpr int kWords = (int)(kPoseHeadBytes / 4);
+  const uint32_t* src = reinterpret_cast<const uint32_t*>(bt->s[slot]->pose);
+  if (threadIdx.x < kWords) out[slot * kWords + threadIdx.x] = src[threadIdx.x];
+}
+
+}  // namespace
+
+void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st) {
+  k_gather_heads<<<kMaxSlots, 32, 0, st>>>(bt, reinterpret_cast<uint32_t*>(out));
+}
+
 int icp_blocks(int npix) {
   int b = (npix + 511) / 512;
   if (b < 1) b = 1;
@@ -543,33 +615,31 @@ int icp_blocks(int npix) {
   return b;
 }
 
-}  // namespace
-
-void launch_icp(const SessionDev* d, const SessionDev& h, cudaStream_t st, bool frame_mode,
-                const float* init_T12) {
-  SessionDev* dm = const_cast<SessionDev*>(d);
+void launch_icp(const BatchTable* bt, int max_levels, const int* max_iters, int reduce_mode, cudaStream_t st,
+                bool frame_mode, const float* init_T12) {
   // frame-level calls skip tracking on the first frame as so_Scan_Object does
   // (zz_flag_track, z_yooji_object_scanner.cpp:534,572-576); explicit
   // tp_Track_Pose calls always track
   const bool with_init = init_T12 != nullptr;
-  k_icp_begin<<<1, 1, 0, st>>>(dm, frame_mode ? 1 : 0, with_init ? 1 : 0, init_T12);
-  for (int l = h.levels - 1; l >= 0; l--) {
-    int nb = icp_blocks(h.lv[l].W * h.lv[l].H);
-    for (int i = 0; i < h.iters[l]; i++) {
-      switch (h.reduce_mode) {
+  k_icp_begin<<<1, kMaxSlots, 0, st>>>(bt, frame_mode ? 1 : 0, with_init ? 1 : 0, init_T12);
+  const int grid = sm_count() * 3 < kIcpMaxBlocks ? sm_count() * 3 : kIcpMaxBlocks;  // 3 resident per SM
+  unsigned* work = const_cast<unsigned*>(bt->work) + 2;
+  for (int l = max_levels - 1; l >= 0; l--) {
+    for (int i = 0; i < max_iters[l]; i++) {
+      switch (reduce_mode) {
         case VS_REDUCE_FP32:
-          k_icp_iter<VS_REDUCE_FP32><<<nb, kThreads, 0, st>>>(d, l);
+          k_icp_iter<VS_REDUCE_FP32><<<grid, kThreads, 0, st>>>(bt, work, l, i);
           break;
         case VS_REDUCE_FP64:
-          k_icp_iter<VS_REDUCE_FP64><<<nb, kThreads, 0, st>>>(d, l);
+          k_icp_iter<VS_REDUCE_FP64><<<grid, kThreads, 0, st>>>(bt, work, l, i);
           break;
         default:
-          k_icp_iter<VS_REDUCE_KAHAN><<<nb, kThreads, 0, st>>>(d, l);
+          k_icp_iter<VS_REDUCE_KAHAN><<<grid, kThreads, 0, st>>>(bt, work, l, i);
           break;
       }
     }
   }
-  k_icp_finish<<<1, 32, 0, st>>>(dm, frame_mode ? 1 : 0);
+  k_icp_finish<<<kMaxSlots, 32, 0, st>>>(bt, frame_mode ? 1 : 0);
 }
 
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st) {

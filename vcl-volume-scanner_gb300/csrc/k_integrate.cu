@@ -15,9 +15,14 @@
 // update kernel is persistent: one warp per listed brick, 16-byte vector
 // loads, 16 voxels per lane.  Flags are cleared by the warp that consumes the
 // brick, so no full-volume pass touches HBM.  Voxel centres and the per-pixel
-// ray scale K^-1 [x y 1] come from shared-memory tables built with the same
-// IEEE operations as the per-voxel reference formula, so the result stays
-// bit-identical while the divisions leave the inner loop.
+// ray scale K^-1 [x y 1] come from per-session tables built once with the
+// same IEEE operations as the per-voxel reference formula, so the result
+// stays bit-identical while the divisions leave the inner loop.
+//
+// Batches: activation is persistent over the level-0 tiles of every session
+// of a batch table, each session filling its own brick list; the update
+// kernel walks the concatenation of the lists (a brick touches only its own
+// session's voxels, so the order across sessions changes no result).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -27,68 +32,147 @@ namespace vs {
 namespace {
 
 constexpr int kIntThreads = 256;
-constexpr int kMaxDimLut = 1024;   // voxels per axis
+constexpr int kMaxDimLut = 1024;   // voxels per axis (bricks fit 21 index bits)
 constexpr int kMaxImgLut = 2048;   // pixels per image axis
 
 // ROUNDF(v)/8 as the unparenthesised reference macro evaluates it
 // (z_yooji_cuda_volume_integrator.cu:133-135)
 __device__ inline int roundf_div8_ref(float x) { return (x < 0.0f) ? (int)(x - 0.5f) : (int)(x + 0.5f) / 8; }
 
-__global__ void k_activate(const SessionDev* __restrict__ s, const float* __restrict__ depth,
-                           const float* __restrict__ Tcg_in, int gate) {
-  if (gate && s->pose->failed) return;
-  const int W = s->lv[0].W, H = s->lv[0].H;
-  int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-  if (x >= W || y >= H) return;
-  float td = depth[(size_t)y * W + x];
-  if (!(td > 0.0f)) return;
-  float T[12];
-#pragma unroll
-  for (int k = 0; k < 12; k++) T[k] = Tcg_in[k];
+// per-session tables: voxel centre coordinate per axis
+// (d_gpw_Get_Position_in_World) and the level-0 ray components K^-1 [x y 1]
+__global__ void k_session_tables(SessionDev* s) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int d0 = s->dim[0], d1 = s->dim[1], d2 = s->dim[2];
+  if (i < d0) s->lut_vox[i] = ((float)i + 0.5f) / s->vox_inv + s->origin[0];
+  if (i < d1) s->lut_vox[d0 + i] = ((float)i + 0.5f) / s->vox_inv + s->origin[1];
+  if (i < d2) s->lut_vox[d0 + d1 + i] = ((float)i + 0.5f) / s->vox_inv + s->origin[2];
   const float* K = s->lv[0].K;
-  F3 p = transform(back_project((float)x, (float)y, K, td), T);
-  F3 pe = transform(back_project((float)x, (float)y, K, 100.0f), T);
-  F3 dv = normalised(sub(pe, p));
-  const int nb0 = s->nb[0], nb1 = s->nb[1], nb2 = s->nb[2];
-  int prev = -1;
-  for (int n = -4; n <= 1; n++) {
-    F3 tp = add(p, scale(((float)n) * s->mu, dv));
-    F3 v;
-    if (!pos_in_voxel(tp, *s, v)) continue;
-    int xs = roundf_div8_ref(v.x), ys = roundf_div8_ref(v.y), zs = roundf_div8_ref(v.z);
-    if (xs < 0 || xs >= nb0 || ys < 0 || ys >= nb1 || zs < 0 || zs >= nb2) break;
-    int b = (zs * nb1 + ys) * nb0 + xs;
-    if (b == prev) continue;
-    prev = b;
-    uint32_t* f = s->brick_flag + b;
-    if (*((volatile uint32_t*)f) == 0u && atomicExch(f, 1u) == 0u) {
-      uint32_t pos = atomicAdd(s->brick_count, 1u);
-      s->brick_list[pos] = (uint32_t)b;
+  if (i < s->lv[0].W) s->lut_ray[i] = 1.0f * ((float)i - K[2]) / K[0];
+  if (i < s->lv[0].H) s->lut_ray[s->lv[0].W + i] = 1.0f * ((float)i - K[3]) / K[1];
+}
+
+// frame counters of every slot
+__global__ void k_integrate_prepare(const BatchTable* __restrict__ bt) {
+  const int i = threadIdx.x;
+  if (i < bt->n) {
+    bt->s[i]->brick_count[0] = 0u;
+    bt->s[i]->brick_count[1] = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_activate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
+                                                  const float* __restrict__ Tcg_ext, int gate) {
+  const int n = bt->n;
+  const int total = bt->bil[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int t;
+    const int slot = find_slot(bt->bil, n, item, t);
+    const SessionDev* __restrict__ s = bt->s[slot];
+    if (gate && s->pose->failed) continue;
+    const int W = s->lv[0].W, H = s->lv[0].H;
+    const int tw = (W + 31) / 32;
+    const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * 8 + threadIdx.y;
+    if (x >= W || y >= H) continue;
+    const float* depth = depth_ext ? depth_ext : s->depth_raw;
+    const float td = depth[(size_t)y * W + x];
+    if (!(td > 0.0f)) continue;
+    const float* Tcg_in = Tcg_ext ? Tcg_ext : s->pose->Tcg;
+    float T[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) T[k] = Tcg_in[k];
+    const float* K = s->lv[0].K;
+    F3 p = transform(back_project((float)x, (float)y, K, td), T);
+    F3 pe = transform(back_project((float)x, (float)y, K, 100.0f), T);
+    F3 dv = normalised(sub(pe, p));
+    const int nb0 = s->nb[0], nb1 = s->nb[1], nb2 = s->nb[2];
+    int prev = -1;
+    for (int m = -4; m <= 1; m++) {
+      F3 tp = add(p, scale(((float)m) * s->mu, dv));
+      F3 v;
+      if (!pos_in_voxel(tp, *s, v)) continue;
+      int xs = roundf_div8_ref(v.x), ys = roundf_div8_ref(v.y), zs = roundf_div8_ref(v.z);
+      if (xs < 0 || xs >= nb0 || ys < 0 || ys >= nb1 || zs < 0 || zs >= nb2) break;
+      int b = (zs * nb1 + ys) * nb0 + xs;
+      if (b == prev) continue;
+      prev = b;
+      uint32_t* f = s->brick_flag + b;
+      if (*((volatile uint32_t*)f) == 0u && atomicExch(f, 1u) == 0u) {
+        uint32_t pos = atomicAdd(s->brick_count, 1u);
+        s->brick_list[pos] = (uint32_t)b;
+      }
     }
   }
 }
 
+// per-warp copy of the session parameters the update needs
+struct IntParams {
+  const float* depth;
+  const float* lut_vox;
+  const float* lut_ray;
+  const uint32_t* list;
+  uint32_t* flag;
+  uint32_t* counters;
+  uint32_t* occ;
+  void* vol;
+  float T[12];
+  float C[3];
+  float K[4];
+  float mu, max_w;
+  int W, H, nb0, nb1, d0, d1;
+};
+
+__device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ s, const float* depth_ext,
+                                   const float* Tgc_ext, const float* Tcg_ext) {
+  q.depth = depth_ext ? depth_ext : s->depth_raw;
+  q.lut_vox = s->lut_vox;
+  q.lut_ray = s->lut_ray;
+  q.list = s->brick_list;
+  q.flag = s->brick_flag;
+  q.counters = s->brick_count;
+  q.occ = s->occ;
+  q.vol = s->vol;
+  const float* Tgc = Tgc_ext ? Tgc_ext : s->pose->Tgc;
+  const float* Tcg = Tcg_ext ? Tcg_ext : s->pose->Tcg;
+#pragma unroll
+  for (int k = 0; k < 12; k++) q.T[k] = Tgc[k];
+  q.C[0] = Tcg[3];
+  q.C[1] = Tcg[7];
+  q.C[2] = Tcg[11];
+#pragma unroll
+  for (int k = 0; k < 4; k++) q.K[k] = s->lv[0].K[k];
+  q.mu = s->mu;
+  q.max_w = s->max_w;
+  q.W = s->lv[0].W;
+  q.H = s->lv[0].H;
+  q.nb0 = s->nb[0];
+  q.nb1 = s->nb[1];
+  q.d0 = s->dim[0];
+  q.d1 = s->dim[1];
+}
+
 template <class S>
 __global__ void __launch_bounds__(kIntThreads)
-    k_integrate(const SessionDev* __restrict__ s, const float* __restrict__ depth,
-                const float* __restrict__ Tgc_in, const float* __restrict__ Tcg_in, int gate) {
-  if (gate && s->pose->failed) return;
-  __shared__ float lut_p[3][kMaxDimLut];  // voxel centre coordinate per axis
-  __shared__ float lut_rx[kMaxImgLut], lut_ry[kMaxImgLut];
-  const int W = s->lv[0].W, H = s->lv[0].H;
-  const float K0 = s->lv[0].K[0], K1 = s->lv[0].K[1], K2 = s->lv[0].K[2], K3 = s->lv[0].K[3];
-  for (int a = 0; a < 3; a++)
-    for (int i = threadIdx.x; i < s->dim[a]; i += blockDim.x)
-      lut_p[a][i] = ((float)i + 0.5f) / s->vox_inv + s->origin[a];  // d_gpw_Get_Position_in_World
-  for (int i = threadIdx.x; i < W; i += blockDim.x) lut_rx[i] = 1.0f * ((float)i - K2) / K0;
-  for (int i = threadIdx.x; i < H; i += blockDim.x) lut_ry[i] = 1.0f * ((float)i - K3) / K1;
-  float T[12];
+    k_integrate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
+                const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext) {
+  __shared__ uint32_t pre[kMaxSlots + 1];  // prefix of the slots' active-brick counts
+  const int n = bt->n;
+  if (threadIdx.x < 32) {
+    const int ln = threadIdx.x;
+    const uint32_t c0 = (2 * ln < n) ? *((volatile uint32_t*)bt->s[2 * ln]->brick_count) : 0u;
+    const uint32_t c1 = (2 * ln + 1 < n) ? *((volatile uint32_t*)bt->s[2 * ln + 1]->brick_count) : 0u;
+    uint32_t v = c0 + c1;
 #pragma unroll
-  for (int k = 0; k < 12; k++) T[k] = Tgc_in[k];
-  const float Cx = Tcg_in[3], Cy = Tcg_in[7], Cz = Tcg_in[11];
-  const float mu = s->mu, max_w = s->max_w;
-  const float K[4] = {K0, K1, K2, K3};
+    for (int m = 1; m < 32; m <<= 1) {
+      const uint32_t o = __shfl_up_sync(0xffffffffu, v, m);
+      if (ln >= m) v += o;
+    }
+    pre[2 * ln + 2] = v;
+    pre[2 * ln + 1] = v - c1;
+    if (ln == 0) pre[0] = 0u;
+  }
   __syncthreads();
+  const uint32_t total = pre[n];
 
   typedef typename S::word word;
   constexpr int kPerVec = 16 / sizeof(word);
@@ -96,16 +180,32 @@ __global__ void __launch_bounds__(kIntThreads)
   const int lane = threadIdx.x & 31;
   const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
-  const uint32_t count = *((volatile uint32_t*)s->brick_count);
-  const int nb0 = s->nb[0], nb1 = s->nb[1];
-  word* vol = reinterpret_cast<word*>(s->vol);
+  IntParams q;
+  int cur = -1;
 
-  for (uint32_t i = gwarp; i < count; i += nwarps) {
-    const uint32_t b = s->brick_list[i];
+  for (uint32_t i = gwarp; i < total; i += nwarps) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (pre[mid] <= i)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    if (lo != cur) {
+      cur = lo;
+      load_params(q, bt->s[lo], depth_ext, Tgc_ext, Tcg_ext);
+    }
+    const uint32_t b = q.list[i - pre[lo]];
     int nupd = 0;
-    const int bx = (int)(b % (uint32_t)nb0), by = (int)((b / (uint32_t)nb0) % (uint32_t)nb1),
-              bz = (int)(b / ((uint32_t)nb0 * (uint32_t)nb1));
-    uint4* bv = reinterpret_cast<uint4*>(vol + (size_t)b * kBrickVox);
+    const int bx = (int)(b % (uint32_t)q.nb0), by = (int)((b / (uint32_t)q.nb0) % (uint32_t)q.nb1),
+              bz = (int)(b / ((uint32_t)q.nb0 * (uint32_t)q.nb1));
+    uint4* bv = reinterpret_cast<uint4*>(reinterpret_cast<word*>(q.vol) + (size_t)b * kBrickVox);
+    const float* __restrict__ lx = q.lut_vox;
+    const float* __restrict__ ly = q.lut_vox + q.d0;
+    const float* __restrict__ lz = q.lut_vox + q.d0 + q.d1;
+    const float* __restrict__ rx_t = q.lut_ray;
+    const float* __restrict__ ry_t = q.lut_ray + q.W;
 #pragma unroll 1
     for (int k = 0; k < kVecs / 32; k++) {
       const int vi = k * 32 + lane;
@@ -121,22 +221,22 @@ __global__ void __launch_bounds__(kIntThreads)
         uint32_t wold;
         S::decode(wv[e], told, wold);
         const float oldW = (float)wold;
-        if (oldW >= max_w) continue;
-        F3 pg = f3(lut_p[0][xc], lut_p[1][yc], lut_p[2][zc]);
-        F3 pc = transform(pg, T);
+        if (oldW >= q.max_w) continue;
+        F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
+        F3 pc = transform(pg, q.T);
         float u, v;
-        project(pc, K, u, v);
+        project(pc, q.K, u, v);
         int x = __float2int_rn(u), y = __float2int_rn(v);
-        if (x < 0 || x > W - 1 || y < 0 || y > H - 1) continue;
-        float dm = __ldg(depth + (size_t)y * W + x);
+        if (x < 0 || x > q.W - 1 || y < 0 || y > q.H - 1) continue;
+        float dm = __ldg(q.depth + (size_t)y * q.W + x);
         if (!(dm > 0.0f)) continue;
-        float rx = lut_rx[x], ry = lut_ry[y];
+        float rx = __ldg(rx_t + x), ry = __ldg(ry_t + y);
         float lam = 1.0f / sqrtf(rx * rx + ry * ry + 1.0f);
-        F3 dc = f3(pg.x - Cx, pg.y - Cy, pg.z - Cz);
+        F3 dc = f3(pg.x - q.C[0], pg.y - q.C[1], pg.z - q.C[2]);
         float nrm = sqrtf(dc.x * dc.x + dc.y * dc.y + dc.z * dc.z);
         float sdf = dm - lam * nrm;
-        if (sdf < -mu) continue;
-        float ts = fminf(1.0f, sdf / mu);
+        if (sdf < -q.mu) continue;
+        float ts = fminf(1.0f, sdf / q.mu);
         float newW = oldW + 1.0f;
         float inewW = 1.0f / newW;
         float tnew = (oldW * told + ts) * inewW;
@@ -152,11 +252,11 @@ __global__ void __launch_bounds__(kIntThreads)
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
     if (lane == 0) {
-      s->brick_flag[b] = 0u;
+      q.flag[b] = 0u;
       if (nupd) {
-        atomicAdd(s->brick_count + 1, (uint32_t)nupd);
+        atomicAdd(q.counters + 1, (uint32_t)nupd);
         // weights never decrease, so a brick that got an update stays occupied
-        if (s->occ) atomicOr(s->occ + (b >> 5), 1u << (b & 31));
+        if (q.occ) atomicOr(q.occ + (b >> 5), 1u << (b & 31));
       }
     }
   }
@@ -222,6 +322,8 @@ __global__ void k_occupancy(const typename S::word* vol, size_t nbr, uint32_t* o
   }
 }
 
+}  // namespace
+
 int sm_count() {
   static int n = 0;
   if (!n) {
@@ -233,24 +335,27 @@ int sm_count() {
   return n;
 }
 
-}  // namespace
+void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) {
+  int m = h.dim[0];
+  for (int v : {h.dim[1], h.dim[2], h.lv[0].W, h.lv[0].H}) m = v > m ? v : m;
+  k_session_tables<<<(m + 255) / 256, 256, 0, st>>>(d);
+}
 
-void launch_integrate(const SessionDev* d, const SessionDev& h, const float* depth, const float* Tgc,
-                      const float* Tcg, bool gate, cudaStream_t st) {
-  cudaMemsetAsync(h.brick_count, 0, 2 * sizeof(uint32_t), st);
-  dim3 b(32, 8), g((h.lv[0].W + 31) / 32, (h.lv[0].H + 7) / 8);
-  k_activate<<<g, b, 0, st>>>(d, depth, Tcg, gate ? 1 : 0);
+void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc, const float* Tcg,
+                      bool gate, cudaStream_t st) {
+  k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt);
+  k_activate<<<sm_count() * 8, dim3(32, 8), 0, st>>>(bt, depth, Tcg, gate ? 1 : 0);
   // persistent grid: enough warps to cover every SM several times over
-  int blocks = sm_count() * 4;
-  switch (h.tsdf_type) {
+  const int blocks = sm_count() * 4;
+  switch (tsdf_type) {
     case VS_TSDF_FP16:
-      k_integrate<StoreF16><<<blocks, kIntThreads, 0, st>>>(d, depth, Tgc, Tcg, gate ? 1 : 0);
+      k_integrate<StoreF16><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
     case VS_TSDF_FP32:
-      k_integrate<StoreF32><<<blocks, kIntThreads, 0, st>>>(d, depth, Tgc, Tcg, gate ? 1 : 0);
+      k_integrate<StoreF32><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
     default:
-      k_integrate<StoreI16><<<blocks, kIntThreads, 0, st>>>(d, depth, Tgc, Tcg, gate ? 1 : 0);
+      k_integrate<StoreI16><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
   }
 }

@@ -3,11 +3,13 @@
 // Reference: g_rmi_Render_Maps_for_ICP, d_crtc_Cast_Ray_on_TSDF_Cube_NEW,
 // d_gtvu / d_gtvi and d_csnt (STAC/Engine/GPU/z_yooji_cuda_tsdf_renderer.cu:
 // 1069-1209, 466-635, 68-153, 288-464; host set-up :1642-1700).  The
-// reference launches one 16x16-block grid per pyramid level; here one launch
-// covers every level (a block is a 16x8 tile of one level), each ray keeps its
-// whole march state in registers, and every voxel read is one 32-bit word that
-// carries both the TSDF value and the weight (one gather instead of the
-// reference's separate float and uchar arrays).
+// reference launches one 16x16-block grid per pyramid level; here one
+// persistent launch covers every level of every session of a batch table
+// (blocks take 16x8 tiles from an atomic work counter, so a slow tile near a
+// surface does not hold up a whole grid row), each ray keeps its whole march
+// state in registers, and every voxel read is one 32-bit word that carries
+// both the TSDF value and the weight (one gather instead of the reference's
+// separate float and uchar arrays).
 //
 // The reference's march loop has no iteration bound: a fine-search ray whose
 // signed steps keep changing direction never leaves it.  The loop here ends
@@ -24,16 +26,15 @@ namespace {
 constexpr int TX = 16, TY = 8;
 
 struct RayArgs {
-  const SessionDev* s;
-  int lev_begin, lev_end;
-  int tiles[kMaxLevels + 1];
+  const BatchTable* bt;
+  unsigned* work;       // [0] next tile, [1] finished blocks; zero between launches
+  int level;            // < 0: every level of every slot into the model maps
+  // explicit poses and outputs of a one-level, one-slot call (reference layout)
   const float* Tgc;
   const float* Tcg;
   const float* center;  // device float[3]
   float light[3];
   int gate;
-  // external outputs in the reference layout (level lev_begin only); NULL =
-  // write the session's model maps
   float* out_depth;
   float* out_vtx3;
   float* out_nrm3;
@@ -231,13 +232,13 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
   return false;
 }
 
+__device__ inline int ray_tiles(const SessionDev& s, int l) {
+  return ((s.lv[l].W + TX - 1) / TX) * ((s.lv[l].H + TY - 1) / TY);
+}
+
 template <class S>
-__global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
-  const SessionDev& s = *a.s;
+__device__ void raycast_tile(const RayArgs& a, const SessionDev& s, int l, int t) {
   if (a.gate && s.pose->failed) return;
-  int b = blockIdx.x, l = a.lev_begin;
-  while (l + 1 < a.lev_end && b >= a.tiles[l + 1 - a.lev_begin]) l++;
-  const int t = b - a.tiles[l - a.lev_begin];
   const int w = s.lv[l].W, h = s.lv[l].H;
   const int tw = (w + TX - 1) / TX;
   const int x = (t % tw) * TX + threadIdx.x, y = (t / tw) * TY + threadIdx.y;
@@ -246,12 +247,16 @@ __global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
   V.v = reinterpret_cast<const typename S::word*>(s.vol);
   V.occ = s.occ;
   for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nb[k] = s.nb[k];
+  const bool ext = a.level >= 0;
+  const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
+  const float* Tcg_in = ext ? a.Tcg : s.pose->Tcg;
+  const float* cen = ext ? a.center : s.pose->center;
   float Tgc[12], Tcg[12], K[4];
 #pragma unroll
-  for (int k = 0; k < 12; k++) Tgc[k] = a.Tgc[k], Tcg[k] = a.Tcg[k];
+  for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k], Tcg[k] = Tcg_in[k];
 #pragma unroll
   for (int k = 0; k < 4; k++) K[k] = s.lv[l].K[k];
-  const F3 cam = f3(a.center[0], a.center[1], a.center[2]);
+  const F3 cam = f3(cen[0], cen[1], cen[2]);
   // host-side set-up of rmi_Render_Maps_for_ICP (:1667-1675)
   const F3 cc = f3(s.cube_center[0], s.cube_center[1], s.cube_center[2]);
   const F3 vcc = sub(cc, cam);
@@ -272,7 +277,7 @@ __global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
     float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
     img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
   }
-  if (a.out_depth) {
+  if (ext) {
     a.out_depth[idx] = dep;
     a.out_vtx3[3 * idx] = pc.x;
     a.out_vtx3[3 * idx + 1] = pc.y;
@@ -287,6 +292,45 @@ __global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
     s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
     s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
     s.m_img[l][idx] = (uint8_t)img;
+  }
+}
+
+template <class S>
+__global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
+  __shared__ int s_item;
+  const BatchTable* __restrict__ bt = a.bt;
+  const int n = bt->n;
+  const int total = (a.level >= 0) ? ray_tiles(*bt->s[0], a.level) : bt->ray[n];
+  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
+  for (;;) {
+    if (lead) s_item = (int)atomicAdd(a.work, 1u);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();  // every thread has the item before the next fetch
+    if (item >= total) break;
+    if (a.level >= 0) {
+      raycast_tile<S>(a, *bt->s[0], a.level, item);
+    } else {
+      int t;
+      const int slot = find_slot(bt->ray, n, item, t);
+      const SessionDev& s = *bt->s[slot];
+      int l = 0;
+      for (; l < s.levels - 1; l++) {
+        const int nt = ray_tiles(s, l);
+        if (t < nt) break;
+        t -= nt;
+      }
+      raycast_tile<S>(a, s, l, t);
+    }
+  }
+  // the last block to finish clears the counters for the next launch
+  if (lead) {
+    __threadfence();
+    if (atomicAdd(a.work + 1, 1u) == gridDim.x - 1) {
+      a.work[0] = 0u;
+      a.work[1] = 0u;
+      __threadfence();
+    }
   }
 }
 
@@ -315,18 +359,25 @@ __global__ void k_maps_export(const float4* __restrict__ mv, const float4* __res
 
 }  // namespace
 
-void launch_raycast(const SessionDev* d, const SessionDev& h, int level_begin, int level_end, const float* Tgc,
-                    const float* Tcg, const float* center, float lx, float ly, float lz, bool gate,
-                    float* out_depth, float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st) {
-  RayArgs a;
-  a.s = d;
-  a.lev_begin = level_begin;
-  a.lev_end = level_end;
-  a.tiles[0] = 0;
-  for (int l = level_begin; l < level_end; l++) {
-    int nt = ((h.lv[l].W + TX - 1) / TX) * ((h.lv[l].H + TY - 1) / TY);
-    a.tiles[l - level_begin + 1] = a.tiles[l - level_begin] + nt;
+int raycast_grid() {
+  static int g = 0;
+  if (!g) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raycast<StoreI16>, TX * TY, 0) != cudaSuccess ||
+        per_sm < 1)
+      per_sm = 4;
+    g = sm_count() * per_sm;
   }
+  return g;
+}
+
+void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
+                    const float* center, float lx, float ly, float lz, bool gate, float* out_depth, float* out_vtx3,
+                    float* out_nrm3, uint8_t* out_img, cudaStream_t st) {
+  RayArgs a;
+  a.bt = bt;
+  a.work = const_cast<unsigned*>(bt->work);
+  a.level = level;
   a.Tgc = Tgc;
   a.Tcg = Tcg;
   a.center = center;
@@ -338,17 +389,17 @@ void launch_raycast(const SessionDev* d, const SessionDev& h, int level_begin, i
   a.out_vtx3 = out_vtx3;
   a.out_nrm3 = out_nrm3;
   a.out_img = out_img;
-  int nblk = a.tiles[level_end - level_begin];
+  const int grid = raycast_grid();
   dim3 blk(TX, TY);
-  switch (h.tsdf_type) {
+  switch (tsdf_type) {
     case VS_TSDF_FP16:
-      k_raycast<StoreF16><<<nblk, blk, 0, st>>>(a);
+      k_raycast<StoreF16><<<grid, blk, 0, st>>>(a);
       break;
     case VS_TSDF_FP32:
-      k_raycast<StoreF32><<<nblk, blk, 0, st>>>(a);
+      k_raycast<StoreF32><<<grid, blk, 0, st>>>(a);
       break;
     default:
-      k_raycast<StoreI16><<<nblk, blk, 0, st>>>(a);
+      k_raycast<StoreI16><<<grid, blk, 0, st>>>(a);
       break;
   }
 }

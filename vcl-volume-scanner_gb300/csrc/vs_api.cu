@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "vs.h"
+#include "vs_host.h"
 #include "vs_internal.cuh"
 
 namespace vs {
@@ -30,22 +31,6 @@ int integrate_max_image();
 }  // namespace vs
 
 using namespace vs;
-
-struct vs_session {
-  vs_config cfg;
-  SessionDev h;          // host copy of the device record
-  SessionDev* d = nullptr;
-  cudaStream_t stream = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  std::vector<void*> allocs;
-  float* stage_f = nullptr;      // level-0 float staging (bfd input)
-  float* dev_small = nullptr;    // 16 floats of scratch (camera centre)
-  Pose* host_pose = nullptr;     // pinned
-  int device = 0;
-  bool timing = false;           // stage events recorded inside the graph
-  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
-};
 
 namespace {
 
@@ -197,14 +182,6 @@ int reset_state(vs_session* s) {
   return VS_OK;
 }
 
-// device addresses of the float pose copies inside the Pose record
-const float* pose_field(const SessionDev& h, size_t off) {
-  return reinterpret_cast<const float*>(reinterpret_cast<const char*>(h.pose) + off);
-}
-#define POSE_TGC(h) pose_field(h, offsetof(Pose, Tgc))
-#define POSE_TCG(h) pose_field(h, offsetof(Pose, Tcg))
-#define POSE_CEN(h) pose_field(h, offsetof(Pose, center))
-
 // the per-frame sequence (recorded into the graph); with stage timing on,
 // event-record nodes separate filter / track / integrate / ray-cast
 void record_frame(vs_session* s, cudaStream_t st) {
@@ -213,15 +190,15 @@ void record_frame(vs_session* s, cudaStream_t st) {
     if (s->timing) cudaEventRecordWithFlags(s->ev[i], st, cudaEventRecordExternal);
   };
   mark(0);
-  launch_filter(s->d, h, st);
-  if (h.cos_normal > -2.0f) launch_input_maps(s->d, h, st);
+  launch_filter(s->tab, st);
+  if (h.cos_normal > -2.0f) launch_input_maps(s->tab, st);
   mark(1);
-  launch_icp(s->d, h, st, true, nullptr);
+  launch_icp(s->tab, h.levels, h.iters, h.reduce_mode, st, true, nullptr);
   mark(2);
-  launch_integrate(s->d, h, h.depth_raw, POSE_TGC(h), POSE_TCG(h), true, st);
+  launch_integrate(s->tab, h.tsdf_type, nullptr, nullptr, nullptr, true, st);
   mark(3);
-  launch_raycast(s->d, h, 0, h.levels, POSE_TGC(h), POSE_TCG(h), POSE_CEN(h), 0.0f, 0.0f, -1.0f, true, nullptr,
-                 nullptr, nullptr, nullptr, st);
+  launch_raycast(s->tab, h.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
+                 nullptr, nullptr, st);
   mark(4);
 }
 
@@ -244,6 +221,8 @@ std::once_flag g_once;
 namespace vs {
 // lets other translation units report through vs_last_error()
 void set_error(const char* msg) { g_err = msg; }
+int fail_code(int code, const std::string& msg) { return fail(code, msg); }
+int cuda_fail_code(cudaError_t e, const char* what) { return cuda_fail(e, what); }
 }  // namespace vs
 
 extern "C" {
@@ -292,7 +271,8 @@ size_t vs_session_bytes(const vs_config* c) {
     size_t n = (size_t)(w >> l) * (h >> l);
     b += n * (4 + 16 + 16 + 1 + 4 + 16 + 16 + 1) + 2 * (size_t)(h >> l) * (((w >> l) + 31) / 32) * 4;
   }
-  b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + 64;
+  b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + sizeof(BatchTable) + 64;
+  b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
   return b;
 }
 
@@ -350,7 +330,10 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.partials, (size_t)kIcpMaxBlocks * kPartials * 16);
   rc |= alloc(s, &h.icp_counter, 64);
   rc |= alloc(s, &h.pose, sizeof(Pose));
+  rc |= alloc(s, &h.lut_vox, (size_t)(h.dim[0] + h.dim[1] + h.dim[2]) * 4);
+  rc |= alloc(s, &h.lut_ray, (size_t)(h.lv[0].W + h.lv[0].H) * 4);
   rc |= alloc(s, &s->d, sizeof(SessionDev));
+  rc |= alloc(s, &s->tab, sizeof(BatchTable));
   if (rc) {
     std::string m = g_err;
     free_all(s);
@@ -358,10 +341,21 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
     return fail(VS_ERR_MEMORY, m);
   }
   e = cudaMemcpy(s->d, &h, sizeof(SessionDev), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    BatchTable t;
+    const SessionDev* hr = &h;
+    const SessionDev* dr = s->d;
+    fill_batch_table(t, &hr, &dr, 1);
+    e = cudaMemcpy(s->tab, &t, sizeof(BatchTable), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) {
+    launch_session_tables(h, s->d, s->stream);
+    e = cudaGetLastError();
+  }
   if (e != cudaSuccess) {
     free_all(s);
     delete s;
-    return cuda_fail(e, "cudaMemcpy(SessionDev)");
+    return cuda_fail(e, "session record set-up");
   }
   rc = reset_state(s);
   if (rc) {
@@ -400,7 +394,7 @@ int vs_bilateral_filter_depth(vs_session* s, float* out_dev, const float* in_hos
   if (!s || !out_dev || !in_host) return fail(VS_ERR_ARG, "null argument");
   if (ww != s->h.lv[0].W || hh != s->h.lv[0].H) return fail(VS_ERR_ARG, "size differs from the session");
   VS_CU(cudaMemcpyAsync(s->stage_f, in_host, (size_t)ww * hh * 4, cudaMemcpyHostToDevice, s->stream));
-  launch_bilateral_float(s->d, s->h, s->stage_f, out_dev, s->stream);
+  launch_bilateral_float(s->h, s->stage_f, out_dev, s->stream);
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
   return VS_OK;
@@ -410,7 +404,7 @@ int vs_bilateral_filter_depth_host(vs_session* s, float* out_host, const float* 
   if (!s || !out_host || !in_host) return fail(VS_ERR_ARG, "null argument");
   if (ww != s->h.lv[0].W || hh != s->h.lv[0].H) return fail(VS_ERR_ARG, "size differs from the session");
   VS_CU(cudaMemcpyAsync(s->stage_f, in_host, (size_t)ww * hh * 4, cudaMemcpyHostToDevice, s->stream));
-  launch_bilateral_float(s->d, s->h, s->stage_f, s->h.depth[0], s->stream);
+  launch_bilateral_float(s->h, s->stage_f, s->h.depth[0], s->stream);
   VS_CU(cudaGetLastError());
   VS_CU(cudaMemcpyAsync(out_host, s->h.depth[0], (size_t)ww * hh * 4, cudaMemcpyDeviceToHost, s->stream));
   VS_CU(cudaStreamSynchronize(s->stream));
@@ -419,7 +413,7 @@ int vs_bilateral_filter_depth_host(vs_session* s, float* out_host, const float* 
 
 int vs_track_pose(vs_session* s, const float* init_T01_dev, int* tracked) {
   if (!s) return fail(VS_ERR_ARG, "null session");
-  launch_icp(s->d, s->h, s->stream, false, init_T01_dev);
+  launch_icp(s->tab, s->h.levels, s->h.iters, s->h.reduce_mode, s->stream, false, init_T01_dev);
   VS_CU(cudaGetLastError());
   VS_CU(cudaMemcpyAsync(s->host_pose, s->h.pose, sizeof(Pose), cudaMemcpyDeviceToHost, s->stream));
   VS_CU(cudaStreamSynchronize(s->stream));
@@ -431,7 +425,7 @@ int vs_integrate_depth(vs_session* s, const float* depth_dev, int ww, int hh, co
                        const float* T_cg_dev) {
   if (!s || !depth_dev || !T_gc_dev || !T_cg_dev) return fail(VS_ERR_ARG, "null argument");
   if (ww != s->h.lv[0].W || hh != s->h.lv[0].H) return fail(VS_ERR_ARG, "size differs from the session");
-  launch_integrate(s->d, s->h, depth_dev, T_gc_dev, T_cg_dev, false, s->stream);
+  launch_integrate(s->tab, s->h.tsdf_type, depth_dev, T_gc_dev, T_cg_dev, false, s->stream);
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
   return VS_OK;
@@ -445,7 +439,7 @@ int vs_render_maps(vs_session* s, int ww, int hh, const float* T_gc_dev, const f
   if (level < 0 || level >= s->h.levels) return fail(VS_ERR_ARG, "bad level");
   if (ww != s->h.lv[level].W || hh != s->h.lv[level].H) return fail(VS_ERR_ARG, "size differs from the level");
   VS_CU(cudaMemcpyAsync(s->dev_small, cam_cen, 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  launch_raycast(s->d, s->h, level, level + 1, T_gc_dev, T_cg_dev, s->dev_small, light[0], light[1], light[2],
+  launch_raycast(s->tab, s->h.tsdf_type, level, T_gc_dev, T_cg_dev, s->dev_small, light[0], light[1], light[2],
                  false, depth_dev, vtx_dev, nrm_dev, img_dev, s->stream);
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
@@ -485,27 +479,27 @@ int vs_stage_filter(vs_session* s, const uint16_t* depth_mm_dev) {
   const size_t n0 = (size_t)s->h.lv[0].W * s->h.lv[0].H;
   if (depth_mm_dev != s->h.depth_mm)
     VS_CU(cudaMemcpyAsync(s->h.depth_mm, depth_mm_dev, n0 * 2, cudaMemcpyDeviceToDevice, s->stream));
-  launch_filter(s->d, s->h, s->stream);
-  if (s->h.cos_normal > -2.0f) launch_input_maps(s->d, s->h, s->stream);
+  launch_filter(s->tab, s->stream);
+  if (s->h.cos_normal > -2.0f) launch_input_maps(s->tab, s->stream);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }
 int vs_stage_track(vs_session* s) {
   if (!s) return fail(VS_ERR_ARG, "null session");
-  launch_icp(s->d, s->h, s->stream, true, nullptr);
+  launch_icp(s->tab, s->h.levels, s->h.iters, s->h.reduce_mode, s->stream, true, nullptr);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }
 int vs_stage_integrate(vs_session* s) {
   if (!s) return fail(VS_ERR_ARG, "null session");
-  launch_integrate(s->d, s->h, s->h.depth_raw, POSE_TGC(s->h), POSE_TCG(s->h), true, s->stream);
+  launch_integrate(s->tab, s->h.tsdf_type, nullptr, nullptr, nullptr, true, s->stream);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }
 int vs_stage_raycast(vs_session* s) {
   if (!s) return fail(VS_ERR_ARG, "null session");
-  launch_raycast(s->d, s->h, 0, s->h.levels, POSE_TGC(s->h), POSE_TCG(s->h), POSE_CEN(s->h), 0.0f, 0.0f, -1.0f,
-                 true, nullptr, nullptr, nullptr, nullptr, s->stream);
+  launch_raycast(s->tab, s->h.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
+                 nullptr, nullptr, s->stream);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }
@@ -676,7 +670,7 @@ int vs_kernels_per_frame(const vs_config* c) {
   if (c->cos_normal > -2.0f) n += 3;        // input maps: pre, row scan, post
   n += 2;                                   // ICP begin / finish
   for (int l = 0; l < c->levels; l++) n += c->icp_iters[l];
-  n += 2;                                   // activation + update
+  n += 3;                                   // counter reset, activation, update
   n += 1;                                   // ray-cast of every level
   return n;
 }

@@ -1,0 +1,361 @@
+// Batch runner (vs_batch_* in include/vs.h): several sessions advanced by one
+// frame each, one launch per stage.
+//
+// The runner owns a device work table and captures the per-frame sequence
+// once; the graph starts with a copy of the table from pinned host memory, so
+// replaying it for another set of sessions only rewrites that host table.  Two
+// pinned tables (and two graph instances, one reading each) alternate, so the
+// host fills step k+1's table while step k runs; the host waits for step k-1
+// before it reuses that step's buffers.  A step ends by gathering every
+// slot's pose head into one buffer that a single copy brings to the host.
+//
+// The graph depends only on the schedule it was captured for: the deepest
+// pyramid and the largest ICP iteration count per level among the sessions,
+// whether any session needs input normal maps, the reduction mode and the
+// TSDF storage.  Sessions with fewer levels or iterations skip the extra
+// launches on the device; a step that needs a longer schedule recaptures.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <string>
+
+#include "vs.h"
+#include "vs_host.h"
+#include "vs_internal.cuh"
+
+using namespace vs;
+
+namespace {
+
+struct Schedule {
+  int levels = 0;
+  int iters[kMaxLevels] = {0, 0, 0};
+  int inmaps = 0;
+  int reduce_mode = -1;
+  int tsdf_type = -1;
+  int timing = 0;
+  bool covers(const Schedule& o) const {
+    if (o.reduce_mode != reduce_mode || o.tsdf_type != tsdf_type || o.timing != timing) return false;
+    if (o.levels > levels || (o.inmaps && !inmaps)) return false;
+    for (int l = 0; l < kMaxLevels; l++)
+      if (o.iters[l] > iters[l]) return false;
+    return true;
+  }
+};
+
+constexpr int kRing = 2;
+
+}  // namespace
+
+struct vs_batch {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  BatchTable* d_tab = nullptr;
+  void* d_heads = nullptr;                     // kMaxSlots pose heads
+  BatchTable* h_tab[kRing] = {nullptr, nullptr};  // pinned
+  unsigned char* h_heads[kRing] = {nullptr, nullptr};  // pinned
+  cudaEvent_t done[kRing] = {nullptr, nullptr};
+  bool used[kRing] = {false, false};
+  cudaGraphExec_t exec[kRing] = {nullptr, nullptr};
+  Schedule sched;
+  int ring = 0;
+  int last = -1;                               // ring slot of the last step
+  int kernels = 0;
+  bool timing = false;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+namespace {
+
+void drop_graphs(vs_batch* b) {
+  for (auto& e : b->exec)
+    if (e) cudaGraphExecDestroy(e), e = nullptr;
+}
+
+void record_step(vs_batch* b, int r, cudaStream_t st) {
+  const Schedule& k = b->sched;
+  auto mark = [&](int i) {
+    if (k.timing) cudaEventRecordWithFlags(b->ev[i], st, cudaEventRecordExternal);
+  };
+  cudaMemcpyAsync(b->d_tab, b->h_tab[r], sizeof(BatchTable), cudaMemcpyHostToDevice, st);
+  mark(0);
+  launch_filter(b->d_tab, st);
+  if (k.inmaps) launch_input_maps(b->d_tab, st);
+  mark(1);
+  launch_icp(b->d_tab, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
+  mark(2);
+  launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st);
+  mark(3);
+  launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
+                 nullptr, nullptr, st);
+  mark(4);
+  launch_gather_heads(b->d_tab, b->d_heads, st);
+  cudaMemcpyAsync(b->h_heads[r], b->d_heads, kMaxSlots * kPoseHeadBytes, cudaMemcpyDeviceToHost, st);
+}
+
+int build_graphs(vs_batch* b) {
+  drop_graphs(b);
+  for (int r = 0; r < kRing; r++) {
+    cudaError_t e = cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return cuda_fail_code(e, "cudaStreamBeginCapture");
+    record_step(b, r, b->stream);
+    cudaGraph_t g = nullptr;
+    e = cudaStreamEndCapture(b->stream, &g);
+    if (e != cudaSuccess) return cuda_fail_code(e, "cudaStreamEndCapture");
+    e = cudaGraphInstantiate(&b->exec[r], g, 0);
+    size_t nn = 0;
+    if (e == cudaSuccess && r == 0) {
+      // kernels per step, for vs_batch_kernels_per_step
+      cudaGraphGetNodes(g, nullptr, &nn);
+      std::vector<cudaGraphNode_t> nodes(nn);
+      cudaGraphGetNodes(g, nodes.data(), &nn);
+      int kc = 0;
+      for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nd, &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) kc++;
+      }
+      b->kernels = kc;
+    }
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return cuda_fail_code(e, "cudaGraphInstantiate");
+  }
+  return VS_OK;
+}
+
+int check_sessions(vs_batch* b, vs_session* const* ss, int n, Schedule& k) {
+  if (n < 1 || n > kMaxSlots) return fail_code(VS_ERR_ARG, "batch size must be 1.." + std::to_string(kMaxSlots));
+  for (int i = 0; i < n; i++) {
+    const vs_session* s = ss[i];
+    if (!s) return fail_code(VS_ERR_ARG, "null session in batch");
+    if (s->device != b->device) return fail_code(VS_ERR_ARG, "sessions of a batch must share the runner's device");
+    for (int j = 0; j < i; j++)
+      if (ss[j] == s) return fail_code(VS_ERR_ARG, "a session appears twice in one batch");
+    const SessionDev& h = s->h;
+    if (i == 0) {
+      k.reduce_mode = h.reduce_mode;
+      k.tsdf_type = h.tsdf_type;
+    } else if (h.reduce_mode != k.reduce_mode || h.tsdf_type != k.tsdf_type) {
+      return fail_code(VS_ERR_ARG, "sessions of a batch must share reduce_mode and tsdf_type");
+    }
+    if (h.levels > k.levels) k.levels = h.levels;
+    for (int l = 0; l < h.levels; l++)
+      if (h.iters[l] > k.iters[l]) k.iters[l] = h.iters[l];
+    if (h.cos_normal > -2.0f) k.inmaps = 1;
+  }
+  k.timing = b->timing ? 1 : 0;
+  return VS_OK;
+}
+
+// fills the next ring slot's table and launches; the frames are already in place
+int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cudaStream_t st, int r) {
+  if (!b->exec[0] || !b->sched.covers(k)) {
+    Schedule m = k;
+    if (b->exec[0] && b->sched.reduce_mode == k.reduce_mode && b->sched.tsdf_type == k.tsdf_type &&
+        b->sched.timing == k.timing) {
+      m.levels = std::max(m.levels, b->sched.levels);
+      m.inmaps |= b->sched.inmaps;
+      for (int l = 0; l < kMaxLevels; l++) m.iters[l] = std::max(m.iters[l], b->sched.iters[l]);
+    }
+    // the graphs read both ring buffers: let in-flight steps finish first
+    cudaError_t e = cudaStreamSynchronize(b->stream);
+    if (e == cudaSuccess && st != b->stream) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail_code(e, "batch schedule change");
+    b->sched = m;
+    int rc = build_graphs(b);
+    if (rc) return rc;
+  }
+  const SessionDev* hr[kMaxSlots];
+  const SessionDev* dr[kMaxSlots];
+  for (int i = 0; i < n; i++) {
+    hr[i] = &ss[i]->h;
+    dr[i] = ss[i]->d;
+  }
+  fill_batch_table(*b->h_tab[r], hr, dr, n);
+  cudaError_t e = cudaGraphLaunch(b->exec[r], st);
+  if (e == cudaSuccess) e = cudaEventRecord(b->done[r], st);
+  if (e != cudaSuccess) return cuda_fail_code(e, "batch step launch");
+  b->used[r] = true;
+  b->last = r;
+  b->ring = (r + 1) % kRing;
+  return VS_OK;
+}
+
+// waits until the ring slot's previous step no longer needs its host buffers
+int claim_slot(vs_batch* b, int& r) {
+  r = b->ring;
+  if (b->used[r]) {
+    cudaError_t e = cudaEventSynchronize(b->done[r]);
+    if (e != cudaSuccess) return cuda_fail_code(e, "batch ring wait");
+  }
+  return VS_OK;
+}
+
+void free_batch(vs_batch* b) {
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graphs(b);
+  for (auto& e : b->ev)
+    if (e) cudaEventDestroy(e), e = nullptr;
+  for (int r = 0; r < kRing; r++) {
+    if (b->done[r]) cudaEventDestroy(b->done[r]);
+    if (b->h_tab[r]) cudaFreeHost(b->h_tab[r]);
+    if (b->h_heads[r]) cudaFreeHost(b->h_heads[r]);
+  }
+  if (b->d_tab) cudaFree(b->d_tab);
+  if (b->d_heads) cudaFree(b->d_heads);
+  if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+}  // namespace
+
+namespace vs {
+
+// host frames -> one step, without waiting; the ring slot tells the caller
+// where the step's pose heads land and which event marks its end
+int batch_launch_host(vs_batch* b, vs_session* const* ss, int n, const uint16_t* const* frames_host, int* ring) {
+  Schedule k;
+  int rc = check_sessions(b, ss, n, k);
+  if (rc) return rc;
+  int r = 0;
+  rc = claim_slot(b, r);
+  if (rc) return rc;
+  for (int i = 0; i < n; i++) {
+    const SessionDev& h = ss[i]->h;
+    cudaError_t e = cudaMemcpyAsync(h.depth_mm, frames_host[i], (size_t)h.lv[0].W * h.lv[0].H * 2,
+                                    cudaMemcpyHostToDevice, b->stream);
+    if (e != cudaSuccess) return cuda_fail_code(e, "batch frame upload");
+  }
+  rc = launch_step(b, ss, n, k, b->stream, r);
+  if (rc) return rc;
+  *ring = r;
+  return VS_OK;
+}
+
+const unsigned char* batch_heads(const vs_batch* b, int r) { return b->h_heads[r]; }
+cudaEvent_t batch_done(const vs_batch* b, int r) { return b->done[r]; }
+
+}  // namespace vs
+
+extern "C" {
+
+int vs_batch_create(vs_batch** out) {
+  if (!out) return fail_code(VS_ERR_ARG, "null output");
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail_code(VS_ERR_CUDA, "no CUDA device available");
+  vs_batch* b = new vs_batch;
+  cudaGetDevice(&b->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_tab, sizeof(BatchTable));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_heads, kMaxSlots * kPoseHeadBytes);
+  for (int r = 0; r < kRing && e == cudaSuccess; r++) {
+    e = cudaMallocHost(&b->h_tab[r], sizeof(BatchTable));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_heads[r], kMaxSlots * kPoseHeadBytes);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done[r], cudaEventDisableTiming);
+    if (e == cudaSuccess) std::memset(b->h_tab[r], 0, sizeof(BatchTable));
+  }
+  if (e != cudaSuccess) {
+    free_batch(b);
+    delete b;
+    return cuda_fail_code(e, "vs_batch_create");
+  }
+  *out = b;
+  return VS_OK;
+}
+
+int vs_batch_destroy(vs_batch* b) {
+  if (!b) return VS_OK;
+  free_batch(b);
+  delete b;
+  return VS_OK;
+}
+
+int vs_batch_step(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_dev,
+                  void* stream) {
+  if (!b || !sessions) return fail_code(VS_ERR_ARG, "null argument");
+  Schedule k;
+  int rc = check_sessions(b, sessions, n, k);
+  if (rc) return rc;
+  cudaStream_t st = stream ? static_cast<cudaStream_t>(stream) : b->stream;
+  int r = 0;
+  rc = claim_slot(b, r);
+  if (rc) return rc;
+  for (int i = 0; i < n; i++) {
+    const uint16_t* src = depth_mm_dev ? depth_mm_dev[i] : nullptr;
+    const SessionDev& h = sessions[i]->h;
+    if (src && src != h.depth_mm) {
+      cudaError_t e = cudaMemcpyAsync(h.depth_mm, src, (size_t)h.lv[0].W * h.lv[0].H * 2, cudaMemcpyDeviceToDevice, st);
+      if (e != cudaSuccess) return cuda_fail_code(e, "batch frame copy");
+    }
+  }
+  return launch_step(b, sessions, n, k, st, r);
+}
+
+int vs_batch_step_host(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_host,
+                       float* T_gc_out, int* tracked_out) {
+  if (!b || !sessions || !depth_mm_host) return fail_code(VS_ERR_ARG, "null argument");
+  Schedule k;
+  int rc = check_sessions(b, sessions, n, k);
+  if (rc) return rc;
+  int r = 0;
+  rc = claim_slot(b, r);
+  if (rc) return rc;
+  for (int i = 0; i < n; i++) {
+    if (!depth_mm_host[i]) return fail_code(VS_ERR_ARG, "null host frame");
+    const SessionDev& h = sessions[i]->h;
+    cudaError_t e = cudaMemcpyAsync(h.depth_mm, depth_mm_host[i], (size_t)h.lv[0].W * h.lv[0].H * 2,
+                                    cudaMemcpyHostToDevice, b->stream);
+    if (e != cudaSuccess) return cuda_fail_code(e, "batch frame upload");
+  }
+  rc = launch_step(b, sessions, n, k, b->stream, r);
+  if (rc) return rc;
+  cudaError_t e = cudaEventSynchronize(b->done[r]);
+  if (e != cudaSuccess) return cuda_fail_code(e, "batch step");
+  for (int i = 0; i < n; i++) {
+    const Pose* p = reinterpret_cast<const Pose*>(b->h_heads[r] + (size_t)i * kPoseHeadBytes);
+    if (T_gc_out) std::memcpy(T_gc_out + 16 * i, p->Tgc, 16 * sizeof(float));
+    if (tracked_out) tracked_out[i] = p->tracked;
+  }
+  return VS_OK;
+}
+
+int vs_batch_sync(vs_batch* b) {
+  if (!b) return fail_code(VS_ERR_ARG, "null batch");
+  for (int r = 0; r < kRing; r++)
+    if (b->used[r]) {
+      cudaError_t e = cudaEventSynchronize(b->done[r]);
+      if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_sync");
+    }
+  cudaError_t e = cudaStreamSynchronize(b->stream);
+  if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_sync");
+  return VS_OK;
+}
+
+int vs_batch_set_stage_timing(vs_batch* b, int enable) {
+  if (!b) return fail_code(VS_ERR_ARG, "null batch");
+  int rc = vs_batch_sync(b);
+  if (rc) return rc;
+  if (enable && !b->ev[0])
+    for (auto& e : b->ev) {
+      cudaError_t c = cudaEventCreate(&e);
+      if (c != cudaSuccess) return cuda_fail_code(c, "cudaEventCreate");
+    }
+  b->timing = enable != 0;
+  return VS_OK;
+}
+
+int vs_batch_get_stage_times(vs_batch* b, float* ms) {
+  if (!b || !ms) return fail_code(VS_ERR_ARG, "null argument");
+  if (!b->timing || !b->sched.timing || b->last < 0) return fail_code(VS_ERR_STATE, "stage timing is off or no step ran");
+  cudaError_t e = cudaEventSynchronize(b->ev[4]);
+  for (int i = 0; i < 4 && e == cudaSuccess; i++) e = cudaEventElapsedTime(ms + i, b->ev[i], b->ev[i + 1]);
+  if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_get_stage_times");
+  return VS_OK;
+}
+
+int vs_batch_kernels_per_step(vs_batch* b) {
+  if (!b) return -1;
+  return b->exec[0] ? b->kernels : -1;
+}
+
+}  // extern "C"

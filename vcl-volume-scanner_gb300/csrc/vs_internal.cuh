@@ -18,8 +18,9 @@ constexpr int kMaxLevels = 3;
 constexpr int kBrick = 8;             // 8^3 voxels per brick = reference sub-cube
 constexpr int kBrickVox = 512;
 constexpr float kQ = 32767.0f;
-constexpr int kPartials = 32;         // doubles per ICP block partial (29 used)
+constexpr int kPartials = 32;         // partial slots per ICP block (29 used)
 constexpr int kIcpMaxBlocks = 456;    // 3 blocks per SM on 152 SMs
+constexpr int kMaxSlots = 64;         // sessions per batched launch
 
 struct Level {
   int W, H;
@@ -85,7 +86,46 @@ struct SessionDev {
   double* partials;              // [kIcpMaxBlocks][2*kPartials]
   unsigned* icp_counter;
   Pose* pose;
+  // tables built once per session with the reference's formulas
+  float* lut_vox;                // voxel centre coordinate per axis: dim[0] + dim[1] + dim[2]
+  float* lut_ray;                // level-0 K^-1 [x 1 1] (W) then [1 y 1] (H) components
 };
+
+// Sessions advanced together by one launch of every per-frame kernel.  The
+// kernels are persistent: a fixed grid walks the work items of all sessions
+// (tiles, ICP block ranges, bricks), mapping an item to (slot, local index)
+// through the prefix arrays, so one captured graph serves any set of
+// sessions.  A session's items and their order do not depend on the other
+// sessions of the table, so every result is the same alone and in a batch.
+// One session alone is a table of one slot.
+struct BatchTable {
+  int n;
+  int pad_;
+  const SessionDev* s[kMaxSlots];
+  int bil[kMaxSlots + 1];              // level-0 32x8 tiles (bilateral, activation)
+  int pyr[kMaxLevels - 1][kMaxSlots + 1];  // 32x8 tiles of levels 1, 2
+  int ipre[kMaxSlots + 1];             // input-map pre-pass 32x8 tiles, all levels
+  int ipost[kMaxSlots + 1];            // input-map post-pass 16x16 tiles, all levels
+  int scan[kMaxSlots + 1];             // input-map row scans: one per level
+  int icp[kMaxLevels][kMaxSlots + 1];  // ICP block ranges per level
+  int ray[kMaxSlots + 1];              // ray-cast 16x8 tiles, all levels
+  unsigned work[4];                    // work counters ([0..1] ray-cast, [2..3] ICP); zero between launches
+};
+
+// slot of work item b (pre: prefix over n slots), or -1 past the last item
+__device__ inline int find_slot(const int* pre, int n, int b, int& local) {
+  if (b >= pre[n]) return -1;
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (pre[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  local = b - pre[lo];
+  return lo;
+}
 
 // ---------------------------------------------------------------------------
 // small float3 helpers (the reference's ITMMath Vector3f operations)
@@ -194,27 +234,36 @@ struct StoreF32 {
 inline size_t voxel_bytes(int tsdf_type) { return tsdf_type == VS_TSDF_FP32 ? 8 : 4; }
 
 // ---------------------------------------------------------------------------
-// launch wrappers (one per kernel file)
+// launch wrappers (one per kernel file).  `bt` is the device table and `hb`
+// its host copy; grids are fixed (persistent), so a captured graph does not
+// depend on the table's contents.
 // ---------------------------------------------------------------------------
-void launch_filter(const SessionDev* d, const SessionDev& h, cudaStream_t st);
-void launch_input_maps(const SessionDev* d, const SessionDev& h, cudaStream_t st);
-void launch_bilateral_float(const SessionDev* d, const SessionDev& h, const float* in, float* out,
-                            cudaStream_t st);
-void launch_icp(const SessionDev* d, const SessionDev& h, cudaStream_t st, bool frame_mode,
-                const float* init_T12_dev);
-void launch_integrate(const SessionDev* d, const SessionDev& h, const float* depth,
-                      const float* Tgc, const float* Tcg, bool gate_on_tracking, cudaStream_t st);
-void launch_raycast(const SessionDev* d, const SessionDev& h, int level_begin, int level_end,
-                    const float* Tgc, const float* Tcg, const float* center, float lx, float ly,
-                    float lz, bool gate_on_tracking, float* out_depth, float* out_vtx3,
-                    float* out_nrm3, uint8_t* out_img, cudaStream_t st);
+int icp_blocks(int npix);
+int sm_count();
+void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n);
+void launch_filter(const BatchTable* bt, cudaStream_t st);
+void launch_input_maps(const BatchTable* bt, cudaStream_t st);
+void launch_bilateral_float(const SessionDev& h, const float* in, float* out, cudaStream_t st);
+// ICP of every slot; the schedule runs levels max_levels-1 .. 0 with
+// max_iters[l] launches each (slots with fewer levels or iterations skip)
+void launch_icp(const BatchTable* bt, int max_levels, const int* max_iters, int reduce_mode, cudaStream_t st,
+                bool frame_mode, const float* init_T12_dev);
+// depth / Tgc / Tcg: explicit inputs of a one-slot table, or NULL for each
+// session's own level-0 depth and pose
+void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc,
+                      const float* Tcg, bool gate_on_tracking, cudaStream_t st);
+// level < 0: every level of every slot into the sessions' model maps; else
+// one level of a one-slot table into the external outputs with explicit poses
+void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
+                    const float* center, float lx, float ly, float lz, bool gate_on_tracking, float* out_depth,
+                    float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st);
+void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st);
 void launch_volume_init(const SessionDev& h, cudaStream_t st);
-void launch_volume_export(const SessionDev& h, float* tsdf, uint16_t* w, cudaStream_t st);
-void launch_volume_import(const SessionDev& h, const float* tsdf, const uint16_t* w,
-                          cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
+// pose heads of every slot, kPoseHeadBytes each, into out (kMaxSlots slots)
+void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st);
 void launch_occupancy_rebuild(const SessionDev& h, cudaStream_t st);
-void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3,
-                        float* inrm3, cudaStream_t st);
+void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3, float* inrm3,
+                        cudaStream_t st);
 
 }  // namespace vs

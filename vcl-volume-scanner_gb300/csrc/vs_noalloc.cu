@@ -13,10 +13,11 @@
 //
 // Scratch: g_noalloc_scratch is a file-scope __device__ array of
 // kNoAllocScratchBytes (about 2 MiB), which every GPU that loads the library
-// holds until the process exits.  It carries the kernel descriptor, the
-// per-sub-cube activation flags, the list of active sub-cubes and the
-// counters, for volumes of up to kNoAllocMaxBricks 8^3 sub-cubes (512^3
-// voxels); larger volumes are rejected with VS_ERR_ARG.  In host code the
+// holds until the process exits.  It carries the kernel descriptor and its
+// one-slot work table, the voxel-centre and ray tables, the per-sub-cube
+// activation flags, the list of active sub-cubes and the counters, for
+// volumes of up to kNoAllocMaxBricks 8^3 sub-cubes (512^3 voxels); larger
+// volumes are rejected with VS_ERR_ARG.  In host code the
 // array's name is only a host-side stand-in, never a device address: its
 // address is obtained once per device with cudaGetSymbolAddress, on the first
 // call made with that device current, and that first call should therefore
@@ -49,9 +50,13 @@ namespace {
 
 constexpr size_t kNoAllocMaxBricks = 262144;  // 512^3 voxels in 8^3 sub-cubes
 constexpr size_t kDescBytes = 2048;           // SessionDev record, padded
+constexpr size_t kTableBytes = 4096;          // one-slot BatchTable, padded
+constexpr size_t kLutBytes = (3 * 1024 + 2 * 2048) * sizeof(float);  // voxel-centre and ray tables
 constexpr size_t kCounterBytes = 256;
-constexpr size_t kNoAllocScratchBytes = kDescBytes + kCounterBytes + 2 * kNoAllocMaxBricks * sizeof(uint32_t);
+constexpr size_t kHeadBytes = kDescBytes + kTableBytes + kLutBytes + kCounterBytes;
+constexpr size_t kNoAllocScratchBytes = kHeadBytes + 2 * kNoAllocMaxBricks * sizeof(uint32_t);
 static_assert(sizeof(SessionDev) <= kDescBytes, "descriptor does not fit its scratch slot");
+static_assert(sizeof(BatchTable) <= kTableBytes, "work table does not fit its scratch slot");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
@@ -122,16 +127,25 @@ extern "C" int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, 
   h.max_w = max_w;
   h.tsdf_type = VS_TSDF_INT16;
   h.vol = volume_dev;
-  h.brick_count = reinterpret_cast<uint32_t*>(sb + kDescBytes);
-  h.brick_flag = reinterpret_cast<uint32_t*>(sb + kDescBytes + kCounterBytes);
+  h.lut_vox = reinterpret_cast<float*>(sb + kDescBytes + kTableBytes);
+  h.lut_ray = h.lut_vox + 3 * 1024;
+  h.brick_count = reinterpret_cast<uint32_t*>(sb + kDescBytes + kTableBytes + kLutBytes);
+  h.brick_flag = reinterpret_cast<uint32_t*>(sb + kHeadBytes);
   h.brick_list = h.brick_flag + kNoAllocMaxBricks;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   SessionDev* d = reinterpret_cast<SessionDev*>(sb);
+  BatchTable* dt = reinterpret_cast<BatchTable*>(sb + kDescBytes);
+  BatchTable t;
+  const SessionDev* hr = &h;
+  const SessionDev* dr = d;
+  fill_batch_table(t, &hr, &dr, 1);
   cudaError_t e = cudaMemcpyAsync(d, &h, sizeof(SessionDev), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(dt, &t, sizeof(BatchTable), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h.brick_flag, 0, nbr * sizeof(uint32_t), st);
   if (e != cudaSuccess) return fail(VS_ERR_CUDA, std::string("scratch set-up: ") + cudaGetErrorString(e));
+  launch_session_tables(h, d, st);
   // counters are cleared inside launch_integrate
-  launch_integrate(d, h, map_depth_dev, T_gc_dev, T_cg_dev, false, st);
+  launch_integrate(dt, VS_TSDF_INT16, map_depth_dev, T_gc_dev, T_cg_dev, false, st);
   e = cudaGetLastError();
   if (e != cudaSuccess) return fail(VS_ERR_CUDA, std::string("integrate launch: ") + cudaGetErrorString(e));
   return VS_OK;

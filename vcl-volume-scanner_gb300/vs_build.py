@@ -19,8 +19,11 @@ BUILD = os.path.join(HERE, "_build")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CXX = os.environ.get("CXX", "g++")
 
-CU_SOURCES = ["k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "vs_api.cu", "vs_noalloc.cu"]
-HEADERS = ["vs_internal.cuh"]
+CU_SOURCES = [
+    "k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "vs_api.cu", "vs_batch.cu", "vs_server.cu",
+    "vs_noalloc.cu",
+]
+HEADERS = ["vs_internal.cuh", "vs_host.h"]
 NVCC_FLAGS = [
     "-gencode", "arch=compute_103a,code=sm_103a",
     "-O3", "-lineinfo", "-std=c++17", "-fmad=false",
@@ -62,7 +65,7 @@ def build(force=False, verbose=False):
             if verbose and out:
                 print(out)
     if force or _stale(LIB, objs):
-        _run([NVCC, "-shared", "-o", LIB] + objs + ["-lcudart"])
+        _run([NVCC, "-shared", "-o", LIB] + objs + ["-lcudart", "-Xcompiler", "-pthread"])
     synth_src = os.path.join(CSRC, "synth.cpp")
     if force or _stale(SYNTH_LIB, [synth_src, os.path.join(CSRC, "vs_synth.h")]):
         _run([CXX, "-O2", "-std=c++17", "-fPIC", "-shared", "-pthread", "-o", SYNTH_LIB, synth_src])

@@ -26,6 +26,8 @@ VS_ERR_ARG = -1
 VS_ERR_CUDA = -2
 VS_ERR_STATE = -3
 VS_ERR_MEMORY = -4
+VS_ERR_BUSY = -5
+VS_MAX_BATCH = 64
 
 VS_TSDF_INT16, VS_TSDF_FP16, VS_TSDF_FP32 = 0, 1, 2
 VS_REDUCE_FP32, VS_REDUCE_KAHAN, VS_REDUCE_FP64 = 0, 1, 2
@@ -76,6 +78,34 @@ class SynthConfig(ctypes.Structure):
     ]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [
+        ("hbm_budget", ctypes.c_size_t),
+        ("max_resident", ctypes.c_int),
+        ("max_batch", ctypes.c_int),
+        ("queue_depth", ctypes.c_int),
+        ("pipeline", ctypes.c_int),
+    ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("session", ctypes.c_int), ("frame", ctypes.c_int), ("tracked", ctypes.c_int), ("batch", ctypes.c_int),
+        ("T_gc", ctypes.c_float * 16),
+        ("t_submit", ctypes.c_double), ("t_done", ctypes.c_double), ("latency_ms", ctypes.c_double),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("steps", ctypes.c_uint64), ("frames", ctypes.c_uint64), ("mean_batch", ctypes.c_double),
+        ("max_batch_seen", ctypes.c_int), ("resident", ctypes.c_int), ("waiting", ctypes.c_int),
+        ("closed", ctypes.c_int), ("bytes_resident", ctypes.c_size_t), ("bytes_budget", ctypes.c_size_t),
+    ]
+
+
+VS_SESSION_WAITING, VS_SESSION_RESIDENT, VS_SESSION_CLOSED = 0, 1, 2
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.POINTER(ctypes.c_float)
@@ -115,6 +145,26 @@ _SIGS = {
     "vs_get_device_buffer": (_I, [_P, _I, ctypes.POINTER(_P)]),
     "vs_integrate_depth_noalloc": (_I, [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _I, _I, _P,
                                         _P, _P, _P]),
+    "vs_batch_create": (_I, [ctypes.POINTER(_P)]),
+    "vs_batch_destroy": (_I, [_P]),
+    "vs_batch_step": (_I, [_P, _P, _I, _P, _P]),
+    "vs_batch_step_host": (_I, [_P, _P, _I, _P, _P, _P]),
+    "vs_batch_sync": (_I, [_P]),
+    "vs_batch_set_stage_timing": (_I, [_P, _I]),
+    "vs_batch_get_stage_times": (_I, [_P, _P]),
+    "vs_batch_kernels_per_step": (_I, [_P]),
+    "vs_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
+    "vs_server_create": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
+    "vs_server_destroy": (_I, [_P]),
+    "vs_server_open": (_I, [_P, ctypes.POINTER(VsConfig), ctypes.POINTER(_I)]),
+    "vs_server_state": (_I, [_P, _I, ctypes.POINTER(_I)]),
+    "vs_server_submit": (_I, [_P, _I, _P]),
+    "vs_server_close": (_I, [_P, _I]),
+    "vs_server_poll": (_I, [_P, ctypes.POINTER(Result), _I, _I]),
+    "vs_server_drain": (_I, [_P]),
+    "vs_server_get_session": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "vs_server_get_stats": (_I, [_P, ctypes.POINTER(ServerStats)]),
+    "vs_server_clock": (ctypes.c_double, []),
 }
 
 _lib = None
@@ -347,6 +397,172 @@ class Session:
         p = ctypes.c_void_p()
         _check(self.lib.vs_get_device_buffer(self.h, which, ctypes.byref(p)))
         return p.value
+
+
+class Batch:
+    """Batch runner: advances several sessions by one frame each per step,
+    one launch per stage for the whole batch (vs_batch_* in include/vs.h)."""
+
+    def __init__(self):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        _check(self.lib.vs_batch_create(ctypes.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.vs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @staticmethod
+    def _handles(sessions):
+        arr = (ctypes.c_void_p * len(sessions))()
+        for i, s in enumerate(sessions):
+            arr[i] = s.h.value if isinstance(s.h, ctypes.c_void_p) else s.h
+        return arr
+
+    def step(self, sessions, depth_mm_dev=None, stream=None):
+        """device frames (integers, or None for frames already in place); returns at once"""
+        hs = self._handles(sessions)
+        frames = None
+        if depth_mm_dev is not None:
+            frames = (ctypes.c_void_p * len(sessions))(*[d if d else None for d in depth_mm_dev])
+        _check(self.lib.vs_batch_step(self.h, hs, len(sessions), frames, _ptr(stream)))
+
+    def step_host(self, sessions, depth_mm):
+        """host uint16 frames in, (T_gc [n,4,4] float32, tracked [n] bool) out"""
+        n = len(sessions)
+        ds = [np.ascontiguousarray(d, dtype=np.uint16) for d in depth_mm]
+        frames = (ctypes.c_void_p * n)(*[d.ctypes.data for d in ds])
+        T = np.empty((n, 16), np.float32)
+        tr = np.empty(n, np.int32)
+        _check(self.lib.vs_batch_step_host(self.h, self._handles(sessions), n, frames, _ptr(T), _ptr(tr)))
+        return T.reshape(n, 4, 4), tr.astype(bool)
+
+    def sync(self):
+        _check(self.lib.vs_batch_sync(self.h))
+
+    def set_stage_timing(self, enable=True):
+        _check(self.lib.vs_batch_set_stage_timing(self.h, 1 if enable else 0))
+
+    def stage_times(self):
+        ms = np.empty(4, np.float32)
+        _check(self.lib.vs_batch_get_stage_times(self.h, _ptr(ms)))
+        return ms
+
+    def kernels_per_step(self):
+        return self.lib.vs_batch_kernels_per_step(self.h)
+
+
+class _Borrowed(Session):
+    """a session owned by a server (state access only; never destroyed here)"""
+
+    def __init__(self, handle, cfg):
+        self.lib = load()
+        self.cfg = cfg
+        self.h = ctypes.c_void_p(handle)
+        self.levels = level_intrinsics(cfg)
+
+    def close(self):
+        self.h = None
+
+
+class Server:
+    """Serving loop: continuous batching of frames from many sessions with
+    admission by HBM budget (vs_server_* in include/vs.h)."""
+
+    def __init__(self, hbm_budget=0, max_resident=0, max_batch=0, queue_depth=0, pipeline=0):
+        self.lib = load()
+        c = ServerConfig()
+        self.lib.vs_server_config_default(ctypes.byref(c))
+        for k, v in dict(hbm_budget=hbm_budget, max_resident=max_resident, max_batch=max_batch,
+                         queue_depth=queue_depth, pipeline=pipeline).items():
+            if v:
+                setattr(c, k, v)
+        h = ctypes.c_void_p()
+        _check(self.lib.vs_server_create(ctypes.byref(c), ctypes.byref(h)))
+        self.h = h
+        self.cfgs = {}
+        self._buf = (Result * 256)()
+
+    def close(self):
+        if self.h:
+            self.lib.vs_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def open(self, cfg):
+        i = _I(0)
+        _check(self.lib.vs_server_open(self.h, ctypes.byref(cfg), ctypes.byref(i)))
+        self.cfgs[i.value] = cfg
+        return i.value
+
+    def state(self, sid):
+        st = _I(0)
+        _check(self.lib.vs_server_state(self.h, sid, ctypes.byref(st)))
+        return st.value
+
+    def submit(self, sid, depth_mm):
+        """returns False when the session's queue is full"""
+        d = np.ascontiguousarray(depth_mm, dtype=np.uint16)
+        rc = self.lib.vs_server_submit(self.h, sid, _ptr(d))
+        if rc == VS_ERR_BUSY:
+            return False
+        _check(rc)
+        return True
+
+    def close_session(self, sid):
+        _check(self.lib.vs_server_close(self.h, sid))
+
+    def poll(self, timeout_ms=0):
+        n = self.lib.vs_server_poll(self.h, self._buf, len(self._buf), int(timeout_ms))
+        if n < 0:
+            _check(n)
+        out = []
+        for r in self._buf[:n]:
+            out.append(dict(session=r.session, frame=r.frame, tracked=bool(r.tracked), batch=r.batch,
+                            T_gc=np.array(r.T_gc, np.float32).reshape(4, 4), t_submit=r.t_submit,
+                            t_done=r.t_done, latency_ms=r.latency_ms))
+        return out
+
+    def drain(self):
+        _check(self.lib.vs_server_drain(self.h))
+
+    def session(self, sid):
+        p = ctypes.c_void_p()
+        _check(self.lib.vs_server_get_session(self.h, sid, ctypes.byref(p)))
+        return _Borrowed(p.value, self.cfgs[sid])
+
+    def stats(self):
+        st = ServerStats()
+        _check(self.lib.vs_server_get_stats(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def clock(self):
+        return self.lib.vs_server_clock()
 
 
 def synth_config(width, height, **kw):
