@@ -389,7 +389,7 @@ void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const 
       const int w = h.lv[l].W, hh = h.lv[l].H;
       ipre += ((w + 31) / 32) * ((hh + 7) / 8);
       ipost += ((w + 15) / 16) * ((hh + 15) / 16);
-      ray += ((w + 15) / 16) * ((hh + 7) / 8);
+      ray += ((w + 7) / 8) * ((hh + 3) / 4);
     }
     hb.bil[i + 1] = hb.bil[i] + ((h.lv[0].W + BX - 1) / BX) * ((h.lv[0].H + BY - 1) / BY);
     for (int l = 1; l < kMaxLevels; l++)

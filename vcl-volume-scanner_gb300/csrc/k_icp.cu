@@ -37,57 +37,72 @@ namespace {
 
 constexpr int kThreads = 256;
 
-__device__ inline bool bilinear4(float xf, float yf, int w, int h, const float4* __restrict__ map, F3& out) {
-  // NaN coordinates are rejected (see the oracle)
+// Bilinear taps of a float4 map at (xf, yf) (d_gii-style interpolation of the
+// reference, _yooji_cuda_math.h:365-481): taps with zero weight are neither
+// tested nor used (they count as 0), a used tap holding the -100 sentinel
+// rejects the sample, and NaN coordinates are rejected (see the oracle).
+// The four reads are issued together; a zero-weight tap reads its row/column
+// neighbour inside the map and is replaced by 0 before use, which gives the
+// read-and-test-in-turn form's result exactly.
+struct Taps {
+  int i00, i01, i10, i11;
+  float rx, ry;
+};
+
+__device__ inline bool tap_setup(float xf, float yf, int w, int h, Taps& t) {
   if (!(xf >= 0.0f && xf <= (float)(w - 1) && yf >= 0.0f && yf <= (float)(h - 1))) return false;
-  int x = (int)xf, y = (int)yf;
-  float rx = xf - (float)x, ry = yf - (float)y;
-  F3 a = f3(0, 0, 0), b = f3(0, 0, 0), c = f3(0, 0, 0), d = f3(0, 0, 0);
-  float4 p = __ldg(map + (size_t)y * w + x);
-  if (p.x == -100.0f) return false;
-  a = f3(p.x, p.y, p.z);
-  if (rx > 0.0f) {
-    p = __ldg(map + (size_t)y * w + x + 1);
-    if (p.x == -100.0f) return false;
-    b = f3(p.x, p.y, p.z);
-  }
-  if (ry > 0.0f) {
-    p = __ldg(map + (size_t)(y + 1) * w + x);
-    if (p.x == -100.0f) return false;
-    c = f3(p.x, p.y, p.z);
-  }
-  if (rx > 0.0f && ry > 0.0f) {
-    p = __ldg(map + (size_t)(y + 1) * w + x + 1);
-    if (p.x == -100.0f) return false;
-    d = f3(p.x, p.y, p.z);
-  }
-  float ix = 1.0f - rx, iy = 1.0f - ry;
-  out.x = iy * (ix * a.x + rx * b.x) + ry * (ix * c.x + rx * d.x);
-  out.y = iy * (ix * a.y + rx * b.y) + ry * (ix * c.y + rx * d.y);
-  out.z = iy * (ix * a.z + rx * b.z) + ry * (ix * c.z + rx * d.z);
+  const int x = (int)xf, y = (int)yf;
+  t.rx = xf - (float)x;
+  t.ry = yf - (float)y;
+  const int xb = t.rx > 0.0f ? x + 1 : x, yb = t.ry > 0.0f ? y + 1 : y;
+  t.i00 = y * w + x;
+  t.i01 = y * w + xb;
+  t.i10 = yb * w + x;
+  t.i11 = yb * w + xb;
   return true;
 }
 
-// d_cssfp_Compute_Single_Summand_with_Forward_Params
+__device__ inline bool interp(const Taps& t, float4 a, float4 b, float4 c, float4 d, F3& out) {
+  const bool ub = t.rx > 0.0f, uc = t.ry > 0.0f, ud = ub && uc;
+  if (a.x == -100.0f || (ub && b.x == -100.0f) || (uc && c.x == -100.0f) || (ud && d.x == -100.0f)) return false;
+  const F3 A = f3(a.x, a.y, a.z);
+  const F3 B = ub ? f3(b.x, b.y, b.z) : f3(0, 0, 0);
+  const F3 C = uc ? f3(c.x, c.y, c.z) : f3(0, 0, 0);
+  const F3 D = ud ? f3(d.x, d.y, d.z) : f3(0, 0, 0);
+  const float rx = t.rx, ry = t.ry, ix = 1.0f - rx, iy = 1.0f - ry;
+  out.x = iy * (ix * A.x + rx * B.x) + ry * (ix * C.x + rx * D.x);
+  out.y = iy * (ix * A.y + rx * B.y) + ry * (ix * C.y + rx * D.y);
+  out.z = iy * (ix * A.z + rx * B.z) + ry * (ix * C.z + rx * D.z);
+  return true;
+}
+
+// d_cssfp_Compute_Single_Summand_with_Forward_Params.  Two rounds of reads:
+// the pixel's depth (and input normal), then the eight model-map taps.
 __device__ inline bool icp_term(int x, int y, int w, int h, const float* K, const float* __restrict__ depth,
                                 const float4* __restrict__ mvtx, const float4* __restrict__ mnrm,
                                 const float4* __restrict__ innrm, const float* T21, float th_icp,
                                 float cos_normal, float A[6], float& b) {
-  float d1 = __ldg(depth + (size_t)y * w + x);
+  const float d1 = __ldg(depth + (size_t)y * w + x);
+  const bool ntest = cos_normal > -2.0f;
+  float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (ntest) q = __ldg(innrm + (size_t)y * w + x);
   if (d1 < 1.0e-6f) return false;
   F3 tp = back_project((float)x, (float)y, K, d1);
   F3 p1 = transform(tp, T21);
   float u, v;
   project(p1, K, u, v);
+  Taps t;
+  if (!tap_setup(u, v, w, h, t)) return false;
+  const float4 va = __ldg(mvtx + t.i00), vb = __ldg(mvtx + t.i01), vc = __ldg(mvtx + t.i10), vd = __ldg(mvtx + t.i11);
+  const float4 na = __ldg(mnrm + t.i00), nb = __ldg(mnrm + t.i01), nc = __ldg(mnrm + t.i10), nd = __ldg(mnrm + t.i11);
   F3 p0;
-  if (!bilinear4(u, v, w, h, mvtx, p0)) return false;
+  if (!interp(t, va, vb, vc, vd, p0)) return false;
   float dd = (p0.x - p1.x) * (p0.x - p1.x) + (p0.y - p1.y) * (p0.y - p1.y) + (p0.z - p1.z) * (p0.z - p1.z);
   if (dd > th_icp) return false;
   F3 n;
-  if (!bilinear4(u, v, w, h, mnrm, n)) return false;
+  if (!interp(t, na, nb, nc, nd, n)) return false;
   n = normalised(n);
-  if (cos_normal > -2.0f) {
-    float4 q = __ldg(innrm + (size_t)y * w + x);
+  if (ntest) {
     if (q.w == 0.0f) return false;
     F3 nin = rotate(f3(q.x, q.y, q.z), T21);
     if (dot(nin, n) < cos_normal) return false;

@@ -114,12 +114,15 @@ struct IntParams {
   uint32_t* flag;
   uint32_t* counters;
   uint32_t* occ;
+  uint32_t* occ1;
+  uint32_t* occ2;
   void* vol;
   float T[12];
   float C[3];
   float K[4];
   float mu, max_w;
   int W, H, nb0, nb1, d0, d1;
+  int nc1[2], nc2[2];
 };
 
 __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ s, const float* depth_ext,
@@ -131,6 +134,12 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.flag = s->brick_flag;
   q.counters = s->brick_count;
   q.occ = s->occ;
+  q.occ1 = s->occ1;
+  q.occ2 = s->occ2;
+  q.nc1[0] = s->nc1[0];
+  q.nc1[1] = s->nc1[1];
+  q.nc2[0] = s->nc2[0];
+  q.nc2[1] = s->nc2[1];
   q.vol = s->vol;
   const float* Tgc = Tgc_ext ? Tgc_ext : s->pose->Tgc;
   const float* Tcg = Tcg_ext ? Tcg_ext : s->pose->Tcg;
@@ -255,8 +264,13 @@ __global__ void __launch_bounds__(kIntThreads)
       q.flag[b] = 0u;
       if (nupd) {
         atomicAdd(q.counters + 1, (uint32_t)nupd);
-        // weights never decrease, so a brick that got an update stays occupied
-        if (q.occ) atomicOr(q.occ + (b >> 5), 1u << (b & 31));
+        // weights never decrease, so a brick that got an update, and the
+        // occupancy cells around it, stay occupied
+        if (q.occ) {
+          set_bit_once(q.occ, b);
+          set_bit_once(q.occ1, occ_cell(bx, by, bz, 2, q.nc1));
+          set_bit_once(q.occ2, occ_cell(bx, by, bz, 4, q.nc2));
+        }
       }
     }
   }
@@ -305,7 +319,10 @@ __global__ void k_volume_import(typename S::word* vol, int X, int Y, int z0, int
 // recomputes the occupancy bits from the weights (after a volume import);
 // one warp per brick
 template <class S>
-__global__ void k_occupancy(const typename S::word* vol, size_t nbr, uint32_t* occ) {
+__global__ void k_occupancy(const SessionDev* __restrict__ s) {
+  const typename S::word* vol = reinterpret_cast<const typename S::word*>(s->vol);
+  const int nb0 = s->nb[0], nb1 = s->nb[1];
+  const size_t nbr = (size_t)nb0 * nb1 * s->nb[2];
   const int lane = threadIdx.x & 31;
   const size_t gw = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const size_t nwarp = ((size_t)gridDim.x * blockDim.x) >> 5;
@@ -318,7 +335,12 @@ __global__ void k_occupancy(const typename S::word* vol, size_t nbr, uint32_t* o
       any |= w != 0u;
     }
     const unsigned m = __ballot_sync(0xffffffffu, any);
-    if (lane == 0 && m) atomicOr(occ + (b >> 5), 1u << (b & 31));
+    if (lane == 0 && m) {
+      const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / ((size_t)nb0 * nb1));
+      set_bit_once(s->occ, (uint32_t)b);
+      set_bit_once(s->occ1, occ_cell(bx, by, bz, 2, s->nc1));
+      set_bit_once(s->occ2, occ_cell(bx, by, bz, 4, s->nc2));
+    }
   }
 }
 
@@ -406,19 +428,30 @@ void launch_volume_slab(const SessionDev& h, bool do_export, int z0, int nz, flo
   }
 }
 
-void launch_occupancy_rebuild(const SessionDev& h, cudaStream_t st) {
-  const size_t nbr = (size_t)h.nb[0] * h.nb[1] * h.nb[2];
-  cudaMemsetAsync(h.occ, 0, ((nbr + 31) / 32) * 4, st);
+size_t occupancy_words(const SessionDev& h, int level) {
+  if (level == 0) return (((size_t)h.nb[0] * h.nb[1] * h.nb[2]) + 31) / 32;
+  const int* nc = level == 1 ? h.nc1 : h.nc2;
+  return (((size_t)nc[0] * nc[1] * nc[2]) + 31) / 32;
+}
+
+void launch_occupancy_clear(const SessionDev& h, cudaStream_t st) {
+  cudaMemsetAsync(h.occ, 0, occupancy_words(h, 0) * 4, st);
+  cudaMemsetAsync(h.occ1, 0, occupancy_words(h, 1) * 4, st);
+  cudaMemsetAsync(h.occ2, 0, occupancy_words(h, 2) * 4, st);
+}
+
+void launch_occupancy_rebuild(const SessionDev& h, const SessionDev* d, cudaStream_t st) {
+  launch_occupancy_clear(h, st);
   const int blocks = sm_count() * 8;
   switch (h.tsdf_type) {
     case VS_TSDF_FP16:
-      k_occupancy<StoreF16><<<blocks, 256, 0, st>>>((const uint32_t*)h.vol, nbr, h.occ);
+      k_occupancy<StoreF16><<<blocks, 256, 0, st>>>(d);
       break;
     case VS_TSDF_FP32:
-      k_occupancy<StoreF32><<<blocks, 256, 0, st>>>((const uint2*)h.vol, nbr, h.occ);
+      k_occupancy<StoreF32><<<blocks, 256, 0, st>>>(d);
       break;
     default:
-      k_occupancy<StoreI16><<<blocks, 256, 0, st>>>((const uint32_t*)h.vol, nbr, h.occ);
+      k_occupancy<StoreI16><<<blocks, 256, 0, st>>>(d);
       break;
   }
 }

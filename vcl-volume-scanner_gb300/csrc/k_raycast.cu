@@ -3,13 +3,16 @@
 // Reference: g_rmi_Render_Maps_for_ICP, d_crtc_Cast_Ray_on_TSDF_Cube_NEW,
 // d_gtvu / d_gtvi and d_csnt (STAC/Engine/GPU/z_yooji_cuda_tsdf_renderer.cu:
 // 1069-1209, 466-635, 68-153, 288-464; host set-up :1642-1700).  The
-// reference launches one 16x16-block grid per pyramid level; here one
-// persistent launch covers every level of every session of a batch table
-// (blocks take 16x8 tiles from an atomic work counter, so a slow tile near a
-// surface does not hold up a whole grid row), each ray keeps its whole march
-// state in registers, and every voxel read is one 32-bit word that carries
-// both the TSDF value and the weight (one gather instead of the reference's
-// separate float and uchar arrays).
+// reference launches one 16x16-block grid per pyramid level; here two
+// persistent launches cover every level of every session of a batch table:
+// k_ray_march marches each ray to its surface point and k_ray_shade computes
+// the surface normal and writes the maps.  Split, each kernel needs far fewer
+// registers than the fused loop, so more warps hide the gather latency.  Each
+// warp takes 8x4-ray tiles from an atomic work counter, so a slow tile near a
+// surface holds up neither a grid row nor the other warps of its block.  A
+// ray keeps its whole march state in registers, and every voxel read is one
+// 32-bit word that carries both the TSDF value and the weight (one gather
+// instead of the reference's separate float and uchar arrays).
 //
 // The reference's march loop has no iteration bound: a fine-search ray whose
 // signed steps keep changing direction never leaves it.  The loop here ends
@@ -23,11 +26,12 @@
 namespace vs {
 namespace {
 
-constexpr int TX = 16, TY = 8;
+constexpr int RX = 8, RY = 4;      // the 32 rays of one warp's tile
+constexpr int kRayThreads = 128;
 
 struct RayArgs {
   const BatchTable* bt;
-  unsigned* work;       // [0] next tile, [1] finished blocks; zero between launches
+  unsigned* work;       // [0] next tile, [1] finished warps; zero between launches
   int level;            // < 0: every level of every slot into the model maps
   // explicit poses and outputs of a one-level, one-slot call (reference layout)
   const float* Tgc;
@@ -49,8 +53,67 @@ template <class S>
 struct Vol {
   const typename S::word* v;
   const uint32_t* occ;
+  const uint32_t* occ1;  // 32^3-voxel cells
+  const uint32_t* occ2;  // 128^3-voxel cells
   int dim[3];
   int nb[3];
+  int nc1[3], nc2[3];
+  __device__ inline bool cell_set(const uint32_t* bits, const int* nc, int shift, int x, int y, int z) const {
+    const uint32_t c = ((uint32_t)(z >> shift) * (uint32_t)nc[1] + (uint32_t)(y >> shift)) * (uint32_t)nc[0] +
+                       (uint32_t)(x >> shift);
+    return (__ldg(bits + (c >> 5)) >> (c & 31)) & 1u;
+  }
+  // Free-space run: how many of the next steps p + k inc (k = 1..m) are
+  // certain to read "no value" - outside the volume, or inside an empty
+  // occupancy cell - so that the march only has to advance the position for
+  // them.  The bounds are pulled in by 0.05 voxel, far more than the
+  // rounding of the position accumulated over a run (at most 64 steps of
+  // float additions, under 1e-2 voxel for coordinates below 2048).
+  __device__ inline int free_run(F3 p, F3 inc) const {
+    if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return 0;
+    const float d = 0.05f;
+    const float pa[3] = {p.x, p.y, p.z}, ia[3] = {inc.x, inc.y, inc.z};
+    // a coordinate is in range iff -0.5 < p < dim - 0.5 (gtvu rounds with ROUNDF)
+    bool inside = true;
+#pragma unroll
+    for (int a = 0; a < 3; a++) inside &= pa[a] > -0.5f && pa[a] < (float)dim[a] - 0.5f;
+    float t;
+    if (!inside) {
+      // outside until every coordinate that is out of range has come in
+      t = 0.0f;
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const float hi = (float)dim[a] - 0.5f;
+        if (pa[a] <= -0.5f)
+          t = fmaxf(t, ia[a] > 0.0f ? (-0.5f - d - pa[a]) / ia[a] : 1e30f);
+        else if (pa[a] >= hi)
+          t = fmaxf(t, ia[a] < 0.0f ? (hi + d - pa[a]) / ia[a] : 1e30f);
+      }
+    } else {
+      const int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
+      int size;
+      if (!cell_set(occ2, nc2, 7, x, y, z))
+        size = 128;
+      else if (!cell_set(occ1, nc1, 5, x, y, z))
+        size = 32;
+      else
+        return 0;
+      const int c[3] = {x & ~(size - 1), y & ~(size - 1), z & ~(size - 1)};
+      t = 1e30f;
+#pragma unroll
+      for (int a = 0; a < 3; a++) {
+        const float lo = (float)c[a] - 0.5f, hi = lo + (float)size;
+        if (ia[a] > 0.0f)
+          t = fminf(t, (hi - d - pa[a]) / ia[a]);
+        else if (ia[a] < 0.0f)
+          t = fminf(t, (lo + d - pa[a]) / ia[a]);
+      }
+    }
+    // steps k >= 1 with k < t
+    t = fminf(t, 65.0f);
+    const int m = (int)ceilf(t) - 1;
+    return m > 0 ? m : 0;
+  }
   __device__ inline bool occupied(int x, int y, int z) const {
     const uint32_t b = ((uint32_t)(z >> 3) * (uint32_t)nb[1] + (uint32_t)(y >> 3)) * (uint32_t)nb[0] + (uint32_t)(x >> 3);
     return (__ldg(occ + (b >> 5)) >> (b & 31)) & 1u;
@@ -69,17 +132,22 @@ struct Vol {
     out = t;
     return true;
   }
-  __device__ inline bool at(int x, int y, int z, float& out) const {
-    if (x < 0 || x >= dim[0] || y < 0 || y >= dim[1] || z < 0 || z >= dim[2]) return false;
-    if (!occupied(x, y, z)) return false;
+  // a voxel read issued without a test in front of it: out-of-range
+  // coordinates read voxel 0 and report invalid, so a group of reads goes to
+  // the memory system back to back instead of one after another.  A voxel of
+  // an unoccupied brick has weight 0, so the weight alone decides (the same
+  // answer as at()).
+  __device__ inline bool at_any(int x, int y, int z, float& out) const {
+    const bool in = x >= 0 && x < dim[0] && y >= 0 && y < dim[1] && z >= 0 && z < dim[2];
     float t;
     uint32_t w;
-    S::decode(__ldg(v + brick_word_index(x, y, z, nb)), t, w);
-    if (w == 0u) return false;
+    S::decode(__ldg(v + (in ? brick_word_index(x, y, z, nb) : 0)), t, w);
     out = t;
-    return true;
+    return in && w != 0u;
   }
-  // d_gtvi_Get_TSDF_Value_Interpolated (offset = floor, see the oracle)
+  // d_gtvi_Get_TSDF_Value_Interpolated (offset = floor, see the oracle); the
+  // eight reads have no side effects, so reading all of them before the
+  // validity test gives the short-circuit form's result
   __device__ inline bool gtvi(F3 p, float& out) const {
     out = 1.0f;
     if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return false;
@@ -87,11 +155,15 @@ struct Vol {
     int ox = (int)fx, oy = (int)fy, oz = (int)fz;
     float rx = p.x - fx, ry = p.y - fy, rz = p.z - fz;
     float f0, f1, f2, f3_, b0, b1, b2, b3;
-    if (!at(ox, oy, oz, f0) || !at(ox + 1, oy, oz, f1) || !at(ox, oy + 1, oz, f2) || !at(ox + 1, oy + 1, oz, f3_))
-      return false;
-    if (!at(ox, oy, oz + 1, b0) || !at(ox + 1, oy, oz + 1, b1) || !at(ox, oy + 1, oz + 1, b2) ||
-        !at(ox + 1, oy + 1, oz + 1, b3))
-      return false;
+    bool ok = at_any(ox, oy, oz, f0);
+    ok &= at_any(ox + 1, oy, oz, f1);
+    ok &= at_any(ox, oy + 1, oz, f2);
+    ok &= at_any(ox + 1, oy + 1, oz, f3_);
+    ok &= at_any(ox, oy, oz + 1, b0);
+    ok &= at_any(ox + 1, oy, oz + 1, b1);
+    ok &= at_any(ox, oy + 1, oz + 1, b2);
+    ok &= at_any(ox + 1, oy + 1, oz + 1, b3);
+    if (!ok) return false;
     float inf = (1.0f - ry) * ((1.0f - rx) * f0 + rx * f1) + ry * ((1.0f - rx) * f2 + rx * f3_);
     float inb = (1.0f - ry) * ((1.0f - rx) * b0 + rx * b1) + ry * ((1.0f - rx) * b2 + rx * b3);
     out = (1.0f - rz) * inf + rz * inb;
@@ -112,19 +184,19 @@ __device__ bool surface_normal(const Vol<S>& V, const SessionDev& s, F3 p3d, F3&
   const int dx1[4] = {0, 1, 0, 1}, dy1[4] = {0, 0, 1, 1};
   const int dx2[12] = {0, 1, -1, 0, 1, 2, -1, 0, 1, 2, 0, 1};
   const int dy2[12] = {-1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2};
+  // all 32 reads are issued before any validity test (no side effects, so
+  // the result equals the reference's read-and-return-early order)
   float fm[4], fr[12], bk[12], bm[4];
+  bool ok = true;
 #pragma unroll
-  for (int i = 0; i < 4; i++)
-    if (!V.at(ox + dx1[i], oy + dy1[i], oz - 1, fm[i])) return false;
+  for (int i = 0; i < 4; i++) ok &= V.at_any(ox + dx1[i], oy + dy1[i], oz - 1, fm[i]);
 #pragma unroll
-  for (int i = 0; i < 12; i++)
-    if (!V.at(ox + dx2[i], oy + dy2[i], oz, fr[i])) return false;
+  for (int i = 0; i < 12; i++) ok &= V.at_any(ox + dx2[i], oy + dy2[i], oz, fr[i]);
 #pragma unroll
-  for (int i = 0; i < 12; i++)
-    if (!V.at(ox + dx2[i], oy + dy2[i], oz + 1, bk[i])) return false;
+  for (int i = 0; i < 12; i++) ok &= V.at_any(ox + dx2[i], oy + dy2[i], oz + 1, bk[i]);
 #pragma unroll
-  for (int i = 0; i < 4; i++)
-    if (!V.at(ox + dx1[i], oy + dy1[i], oz + 2, bm[i])) return false;
+  for (int i = 0; i < 4; i++) ok &= V.at_any(ox + dx1[i], oy + dy1[i], oz + 2, bm[i]);
+  if (!ok) return false;
   float a4[4], b4[4], a2[2], b2[2], gx, gy, gz;
   a4[0] = (1.0f - rz) * fr[2] + rz * bk[2];
   a4[1] = (1.0f - rz) * fr[3] + rz * bk[3];
@@ -219,6 +291,19 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
         state = FINE;
       }
     }
+    if (tsdf == 1.0f && state != BEHIND) {
+      // While samples read "no value" (TSDF 1) the state and the step stay as
+      // they are, so the steps of a free-space run are replayed with the same
+      // float operations as the loop above, without the volume reads.
+      const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
+      const F3 inc = scale(sn, rd);
+      for (int m = V.free_run(vs, inc); m > 0; m--) {
+        if (++it > cap) return false;
+        vs = add(vs, inc);
+        total += sn;
+        if (total > total_max) return false;
+      }
+    }
   }
   if (state == BEHIND) {
     step = step_scale * tsdf;
@@ -233,105 +318,151 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
 }
 
 __device__ inline int ray_tiles(const SessionDev& s, int l) {
-  return ((s.lv[l].W + TX - 1) / TX) * ((s.lv[l].H + TY - 1) / TY);
+  return ((s.lv[l].W + RX - 1) / RX) * ((s.lv[l].H + RY - 1) / RY);
 }
 
-template <class S>
-__device__ void raycast_tile(const RayArgs& a, const SessionDev& s, int l, int t) {
-  if (a.gate && s.pose->failed) return;
-  const int w = s.lv[l].W, h = s.lv[l].H;
-  const int tw = (w + TX - 1) / TX;
-  const int x = (t % tw) * TX + threadIdx.x, y = (t / tw) * TY + threadIdx.y;
-  if (x >= w || y >= h) return;
-  Vol<S> V;
-  V.v = reinterpret_cast<const typename S::word*>(s.vol);
-  V.occ = s.occ;
-  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nb[k] = s.nb[k];
-  const bool ext = a.level >= 0;
-  const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
-  const float* Tcg_in = ext ? a.Tcg : s.pose->Tcg;
-  const float* cen = ext ? a.center : s.pose->center;
-  float Tgc[12], Tcg[12], K[4];
-#pragma unroll
-  for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k], Tcg[k] = Tcg_in[k];
-#pragma unroll
-  for (int k = 0; k < 4; k++) K[k] = s.lv[l].K[k];
-  const F3 cam = f3(cen[0], cen[1], cen[2]);
-  // host-side set-up of rmi_Render_Maps_for_ICP (:1667-1675)
-  const F3 cc = f3(s.cube_center[0], s.cube_center[1], s.cube_center[2]);
-  const F3 vcc = sub(cc, cam);
-  const F3 ncc = normalised(vcc);
-  const float dist_cc = length(vcc);
-  const float theta_max = asinf(s.r_cube / dist_cc);
-
-  F3 pg, sn;
-  bool valid = cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, ncc, dist_cc, theta_max, pg);
-  if (valid) valid = surface_normal(V, s, pg, sn);
-  const size_t idx = (size_t)y * w + x;
-  float dep = 0.0f, img = 0.0f;
-  F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
-  if (valid) {
-    pc = transform(pg, Tgc);
-    dep = pc.z;
-    sc = rotate(sn, Tgc);
-    float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
-    img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
-  }
-  if (ext) {
-    a.out_depth[idx] = dep;
-    a.out_vtx3[3 * idx] = pc.x;
-    a.out_vtx3[3 * idx + 1] = pc.y;
-    a.out_vtx3[3 * idx + 2] = pc.z;
-    a.out_nrm3[3 * idx] = sc.x;
-    a.out_nrm3[3 * idx + 1] = sc.y;
-    a.out_nrm3[3 * idx + 2] = sc.z;
-    if (a.out_img) a.out_img[idx] = (uint8_t)img;
-  } else {
-    float vw = valid ? 1.0f : 0.0f;
-    s.m_depth[l][idx] = dep;
-    s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
-    s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
-    s.m_img[l][idx] = (uint8_t)img;
-  }
-}
-
-template <class S>
-__global__ void __launch_bounds__(TX* TY) k_raycast(RayArgs a) {
-  __shared__ int s_item;
+// Hands the calling warp 8x4-ray tiles until none are left and calls
+// f(session, level, x, y) for each lane's pixel inside its level.  The last
+// warp to finish clears the counters for the next launch.
+template <class F>
+__device__ inline void for_each_ray_tile(const RayArgs& a, F&& f) {
   const BatchTable* __restrict__ bt = a.bt;
+  const int lane = threadIdx.x & 31;
   const int n = bt->n;
   const int total = (a.level >= 0) ? ray_tiles(*bt->s[0], a.level) : bt->ray[n];
-  const bool lead = threadIdx.x == 0 && threadIdx.y == 0;
   for (;;) {
-    if (lead) s_item = (int)atomicAdd(a.work, 1u);
-    __syncthreads();
-    const int item = s_item;
-    __syncthreads();  // every thread has the item before the next fetch
+    int item = 0;
+    if (lane == 0) item = (int)atomicAdd(a.work, 1u);
+    item = __shfl_sync(0xffffffffu, item, 0);
     if (item >= total) break;
+    int t, l, slot;
     if (a.level >= 0) {
-      raycast_tile<S>(a, *bt->s[0], a.level, item);
+      slot = 0;
+      l = a.level;
+      t = item;
     } else {
-      int t;
-      const int slot = find_slot(bt->ray, n, item, t);
+      slot = find_slot(bt->ray, n, item, t);
       const SessionDev& s = *bt->s[slot];
-      int l = 0;
+      l = 0;
       for (; l < s.levels - 1; l++) {
         const int nt = ray_tiles(s, l);
         if (t < nt) break;
         t -= nt;
       }
-      raycast_tile<S>(a, s, l, t);
     }
+    const SessionDev& s = *bt->s[slot];
+    if (a.gate && s.pose->failed) continue;
+    const int tw = (s.lv[l].W + RX - 1) / RX;
+    const int x = (t % tw) * RX + (lane & (RX - 1)), y = (t / tw) * RY + (lane / RX);
+    if (x < s.lv[l].W && y < s.lv[l].H) f(s, l, x, y);
   }
-  // the last block to finish clears the counters for the next launch
-  if (lead) {
+  if (lane == 0) {
     __threadfence();
-    if (atomicAdd(a.work + 1, 1u) == gridDim.x - 1) {
+    const unsigned warps = gridDim.x * (blockDim.x >> 5);
+    if (atomicAdd(a.work + 1, 1u) == warps - 1) {
       a.work[0] = 0u;
       a.work[1] = 0u;
       __threadfence();
     }
   }
+}
+
+// offset of level l's pixels in the per-session hit buffer
+__device__ inline size_t hit_offset(const SessionDev& s, int l) {
+  size_t o = 0;
+  for (int k = 0; k < l; k++) o += (size_t)s.lv[k].W * s.lv[k].H;
+  return o;
+}
+
+template <class S>
+__device__ inline Vol<S> volume_of(const SessionDev& s) {
+  Vol<S> V;
+  V.v = reinterpret_cast<const typename S::word*>(s.vol);
+  V.occ = s.occ;
+  V.occ1 = s.occ1;
+  V.occ2 = s.occ2;
+  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nb[k] = s.nb[k], V.nc1[k] = s.nc1[k], V.nc2[k] = s.nc2[k];
+  return V;
+}
+
+#ifndef VS_RAY_MIN_BLOCKS
+#define VS_RAY_MIN_BLOCKS 8  // resident 128-thread blocks per SM the register allocation must allow
+#endif
+#ifndef VS_SHADE_MIN_BLOCKS
+#define VS_SHADE_MIN_BLOCKS 8
+#endif
+
+// phase 1: march every ray to its surface point (global coordinates; w = 1
+// hit, 0 none) in the session's hit buffer
+template <class S>
+__global__ void __launch_bounds__(kRayThreads, VS_RAY_MIN_BLOCKS) k_ray_march(RayArgs a) {
+  for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
+    const Vol<S> V = volume_of<S>(s);
+    const bool ext = a.level >= 0;
+    const float* Tcg_in = ext ? a.Tcg : s.pose->Tcg;
+    const float* cen = ext ? a.center : s.pose->center;
+    float Tcg[12], K[4];
+#pragma unroll
+    for (int k = 0; k < 12; k++) Tcg[k] = Tcg_in[k];
+#pragma unroll
+    for (int k = 0; k < 4; k++) K[k] = s.lv[l].K[k];
+    const F3 cam = f3(cen[0], cen[1], cen[2]);
+    // host-side set-up of rmi_Render_Maps_for_ICP (:1667-1675)
+    const F3 cc = f3(s.cube_center[0], s.cube_center[1], s.cube_center[2]);
+    const F3 vcc = sub(cc, cam);
+    const F3 ncc = normalised(vcc);
+    const float dist_cc = length(vcc);
+    const float theta_max = asinf(s.r_cube / dist_cc);
+    F3 pg;
+    const bool hit = cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, ncc, dist_cc, theta_max, pg);
+    s.ray_hit[hit_offset(s, l) + (size_t)y * s.lv[l].W + x] =
+        hit ? make_float4(pg.x, pg.y, pg.z, 1.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  });
+}
+
+// phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
+// normal, shading, into the model maps or the external outputs
+template <class S>
+__global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(RayArgs a) {
+  for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
+    const Vol<S> V = volume_of<S>(s);
+    const bool ext = a.level >= 0;
+    const size_t idx = (size_t)y * s.lv[l].W + x;
+    const float4 h = s.ray_hit[hit_offset(s, l) + idx];
+    const F3 pg = f3(h.x, h.y, h.z);
+    F3 sn;
+    bool valid = h.w != 0.0f;
+    if (valid) valid = surface_normal(V, s, pg, sn);
+    float dep = 0.0f, img = 0.0f;
+    F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
+    if (valid) {
+      const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
+      float Tgc[12];
+#pragma unroll
+      for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k];
+      pc = transform(pg, Tgc);
+      dep = pc.z;
+      sc = rotate(sn, Tgc);
+      float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
+      img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
+    }
+    if (ext) {
+      a.out_depth[idx] = dep;
+      a.out_vtx3[3 * idx] = pc.x;
+      a.out_vtx3[3 * idx + 1] = pc.y;
+      a.out_vtx3[3 * idx + 2] = pc.z;
+      a.out_nrm3[3 * idx] = sc.x;
+      a.out_nrm3[3 * idx + 1] = sc.y;
+      a.out_nrm3[3 * idx + 2] = sc.z;
+      if (a.out_img) a.out_img[idx] = (uint8_t)img;
+    } else {
+      const float vw = valid ? 1.0f : 0.0f;
+      s.m_depth[l][idx] = dep;
+      s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
+      s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
+      s.m_img[l][idx] = (uint8_t)img;
+    }
+  });
 }
 
 __global__ void k_maps_export(const float4* __restrict__ mv, const float4* __restrict__ mn,
@@ -359,16 +490,22 @@ __global__ void k_maps_export(const float4* __restrict__ mv, const float4* __res
 
 }  // namespace
 
-int raycast_grid() {
-  static int g = 0;
-  if (!g) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_raycast<StoreI16>, TX * TY, 0) != cudaSuccess ||
-        per_sm < 1)
-      per_sm = 4;
-    g = sm_count() * per_sm;
-  }
-  return g;
+template <class K>
+int resident_grid(K kernel) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRayThreads, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 4;
+  return sm_count() * per_sm;
+}
+
+template <class S>
+void launch_ray_phases(const RayArgs& a0, cudaStream_t st) {
+  static const int g_march = resident_grid(k_ray_march<S>);
+  static const int g_shade = resident_grid(k_ray_shade<S>);
+  RayArgs a = a0;
+  k_ray_march<S><<<g_march, kRayThreads, 0, st>>>(a);
+  a.work = a0.work + 4;
+  k_ray_shade<S><<<g_shade, kRayThreads, 0, st>>>(a);
 }
 
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
@@ -376,7 +513,7 @@ void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float*
                     float* out_nrm3, uint8_t* out_img, cudaStream_t st) {
   RayArgs a;
   a.bt = bt;
-  a.work = const_cast<unsigned*>(bt->work);
+  a.work = const_cast<unsigned*>(bt->work);  // [0..1] march, [4..5] shade
   a.level = level;
   a.Tgc = Tgc;
   a.Tcg = Tcg;
@@ -389,17 +526,15 @@ void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float*
   a.out_vtx3 = out_vtx3;
   a.out_nrm3 = out_nrm3;
   a.out_img = out_img;
-  const int grid = raycast_grid();
-  dim3 blk(TX, TY);
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      k_raycast<StoreF16><<<grid, blk, 0, st>>>(a);
+      launch_ray_phases<StoreF16>(a, st);
       break;
     case VS_TSDF_FP32:
-      k_raycast<StoreF32><<<grid, blk, 0, st>>>(a);
+      launch_ray_phases<StoreF32>(a, st);
       break;
     default:
-      k_raycast<StoreI16><<<grid, blk, 0, st>>>(a);
+      launch_ray_phases<StoreI16>(a, st);
       break;
   }
 }

@@ -94,6 +94,8 @@ void fill_geometry(const vs_config* c, SessionDev& h) {
   for (int k = 0; k < 3; k++) {
     h.dim[k] = c->dim[k];
     h.nb[k] = c->dim[k] / 8;
+    h.nc1[k] = (h.nb[k] + 3) / 4;
+    h.nc2[k] = (h.nb[k] + 15) / 16;
     h.origin[k] = c->origin[k];
   }
   h.vox = c->voxel_size;
@@ -155,7 +157,8 @@ int reset_state(vs_session* s) {
   VS_CU(cudaMemsetAsync(s->h.brick_flag, 0, sizeof(uint32_t) * (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2],
                         s->stream));
   VS_CU(cudaMemsetAsync(s->h.brick_count, 0, sizeof(uint32_t), s->stream));
-  VS_CU(cudaMemsetAsync(s->h.occ, 0, (((size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2] + 31) / 32) * 4, s->stream));
+  launch_occupancy_clear(s->h, s->stream);
+  VS_CU(cudaGetLastError());
   VS_CU(cudaMemsetAsync(s->h.icp_counter, 0, sizeof(unsigned), s->stream));
   Pose p;
   std::memset(&p, 0, sizeof(p));
@@ -264,7 +267,7 @@ size_t vs_session_bytes(const vs_config* c) {
   if (check_config(c) != VS_OK) return 0;
   size_t b = volume_bytes(c);
   size_t nbr = (size_t)(c->dim[0] / 8) * (c->dim[1] / 8) * (c->dim[2] / 8);
-  b += 2 * nbr * 4 + ((nbr + 31) / 32) * 4 + 64;
+  b += 2 * nbr * 4 + 3 * (((nbr + 31) / 32) * 4) + 64;
   int w = c->width, h = c->height;
   b += (size_t)w * h * (2 + 4 + 4);
   for (int l = 0; l < c->levels; l++) {
@@ -273,6 +276,7 @@ size_t vs_session_bytes(const vs_config* c) {
   }
   b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + sizeof(BatchTable) + 64;
   b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
+  for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
   return b;
 }
 
@@ -309,7 +313,9 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.brick_flag, nbr * 4);
   rc |= alloc(s, &h.brick_list, nbr * 4);
   rc |= alloc(s, &h.brick_count, 64);
-  rc |= alloc(s, &h.occ, ((nbr + 31) / 32) * 4);
+  rc |= alloc(s, &h.occ, occupancy_words(h, 0) * 4);
+  rc |= alloc(s, &h.occ1, occupancy_words(h, 1) * 4);
+  rc |= alloc(s, &h.occ2, occupancy_words(h, 2) * 4);
   rc |= alloc(s, &h.depth_mm, n0 * 2);
   rc |= alloc(s, &h.depth_raw, n0 * 4);
   rc |= alloc(s, &s->stage_f, n0 * 4);
@@ -332,6 +338,11 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.pose, sizeof(Pose));
   rc |= alloc(s, &h.lut_vox, (size_t)(h.dim[0] + h.dim[1] + h.dim[2]) * 4);
   rc |= alloc(s, &h.lut_ray, (size_t)(h.lv[0].W + h.lv[0].H) * 4);
+  {
+    size_t npx = 0;
+    for (int l = 0; l < h.levels; l++) npx += (size_t)h.lv[l].W * h.lv[l].H;
+    rc |= alloc(s, &h.ray_hit, npx * sizeof(float4));
+  }
   rc |= alloc(s, &s->d, sizeof(SessionDev));
   rc |= alloc(s, &s->tab, sizeof(BatchTable));
   if (rc) {
@@ -565,7 +576,7 @@ static int volume_transfer(vs_session* s, bool do_export, float* tsdf, uint16_t*
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
   }
   if (e == cudaSuccess && !do_export) {
-    launch_occupancy_rebuild(s->h, s->stream);
+    launch_occupancy_rebuild(s->h, s->d, s->stream);
     e = cudaStreamSynchronize(s->stream);
   }
   cudaFree(dt);
@@ -671,7 +682,7 @@ int vs_kernels_per_frame(const vs_config* c) {
   n += 2;                                   // ICP begin / finish
   for (int l = 0; l < c->levels; l++) n += c->icp_iters[l];
   n += 3;                                   // counter reset, activation, update
-  n += 1;                                   // ray-cast of every level
+  n += 2;                                   // ray march + shading of every level
   return n;
 }
 

@@ -82,6 +82,9 @@ struct SessionDev {
   uint32_t* brick_list;          // active bricks of this frame
   uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame)
   uint32_t* occ;                 // 1 bit per brick: some voxel has weight > 0 (NULL: not kept)
+  uint32_t* occ1;                // 1 bit per 4^3 bricks (32^3 voxels): some brick occupied
+  uint32_t* occ2;                // 1 bit per 16^3 bricks (128^3 voxels)
+  int nc1[3], nc2[3];            // cells per axis of occ1 / occ2
   // ICP scratch
   double* partials;              // [kIcpMaxBlocks][2*kPartials]
   unsigned* icp_counter;
@@ -89,6 +92,7 @@ struct SessionDev {
   // tables built once per session with the reference's formulas
   float* lut_vox;                // voxel centre coordinate per axis: dim[0] + dim[1] + dim[2]
   float* lut_ray;                // level-0 K^-1 [x 1 1] (W) then [1 y 1] (H) components
+  float4* ray_hit;               // ray-cast surface points, every level's pixels in turn
 };
 
 // Sessions advanced together by one launch of every per-frame kernel.  The
@@ -108,8 +112,9 @@ struct BatchTable {
   int ipost[kMaxSlots + 1];            // input-map post-pass 16x16 tiles, all levels
   int scan[kMaxSlots + 1];             // input-map row scans: one per level
   int icp[kMaxLevels][kMaxSlots + 1];  // ICP block ranges per level
-  int ray[kMaxSlots + 1];              // ray-cast 16x8 tiles, all levels
-  unsigned work[4];                    // work counters ([0..1] ray-cast, [2..3] ICP); zero between launches
+  int ray[kMaxSlots + 1];              // ray-cast 8x4 tiles, all levels
+  unsigned work[8];                    // work counters ([0..1] ray march, [2..3] ICP, [4..5] ray
+                                       // shading); zero between launches
 };
 
 // slot of work item b (pre: prefix over n slots), or -1 past the last item
@@ -187,6 +192,20 @@ __device__ inline F3 pos_in_world(F3 v, const SessionDev& s) {
 // Bricks are 512 consecutive words, x fastest inside the brick; bricks are
 // ordered x fastest, then y, then z.
 // ---------------------------------------------------------------------------
+// occupancy cell index of brick (bx, by, bz) at level `shift` (2: 4^3
+// bricks, 4: 16^3 bricks) in a grid of nc cells per axis
+__host__ __device__ inline uint32_t occ_cell(int bx, int by, int bz, int shift, const int* nc) {
+  return ((uint32_t)(bz >> shift) * (uint32_t)nc[1] + (uint32_t)(by >> shift)) * (uint32_t)nc[0] +
+         (uint32_t)(bx >> shift);
+}
+
+// sets bit i of a bitmap unless it is set already (the test keeps the atomics
+// off words whose bits all settled in earlier frames)
+__device__ inline void set_bit_once(uint32_t* bits, uint32_t i) {
+  const uint32_t m = 1u << (i & 31);
+  if (!(*((volatile uint32_t*)bits + (i >> 5)) & m)) atomicOr(bits + (i >> 5), m);
+}
+
 __host__ __device__ inline size_t brick_word_index(int x, int y, int z, const int* nb) {
   size_t b = ((size_t)(z >> 3) * nb[1] + (size_t)(y >> 3)) * nb[0] + (size_t)(x >> 3);
   return b * kBrickVox + (size_t)(((z & 7) << 6) | ((y & 7) << 3) | (x & 7));
@@ -262,7 +281,9 @@ void launch_volume_init(const SessionDev& h, cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
 // pose heads of every slot, kPoseHeadBytes each, into out (kMaxSlots slots)
 void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st);
-void launch_occupancy_rebuild(const SessionDev& h, cudaStream_t st);
+size_t occupancy_words(const SessionDev& h, int level);  // level 0: bricks, 1: 4^3, 2: 16^3 bricks
+void launch_occupancy_clear(const SessionDev& h, cudaStream_t st);
+void launch_occupancy_rebuild(const SessionDev& h, const SessionDev* d, cudaStream_t st);
 void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3, float* inrm3,
                         cudaStream_t st);
 

@@ -18,7 +18,7 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libvs_gb300.so")
+LIB_PATH = os.environ.get("VS_LIB", os.path.join(HERE, "libvs_gb300.so"))
 SYNTH_PATH = os.path.join(HERE, "libvs_synth.so")
 
 VS_OK = 0
