@@ -126,64 +126,105 @@ __device__ inline void two_sum(float a, float b, float& s, float& e) {
 
 // Per-thread sums of the (few) pixels a thread owns are plain float (FP32
 // and compensated modes) or double (FP64 mode); the compensated mode carries
-// (sum, error) pairs only from the warp shuffle tree on, where thousands of
+// (sum, error) pairs only from the warp reduction on, where thousands of
 // values meet, so the pixel loop keeps 29 accumulators in registers.
+//
+// Warp reduction: a butterfly reduce-scatter over the 29 sums (padded to
+// 32).  At the level of lane bit m every lane keeps one half of its current
+// values, sends the other half to lane ^ m and adds what it receives, so the
+// five levels cost 16 + 8 + 4 + 2 + 1 exchanges instead of 29 per level, and
+// lane q ends with the warp's sum of quantity q, in a fixed order.
+template <int HALF, int M, class T>
+__device__ __forceinline__ void rs_level(T* a, int lane) {
+  const bool hi = (lane & M) != 0;
+#pragma unroll
+  for (int i = 0; i < HALF; i++) {
+    const T keep = hi ? a[HALF + i] : a[i];
+    const T send = hi ? a[i] : a[HALF + i];
+    a[i] = keep + __shfl_xor_sync(0xffffffffu, send, M);
+  }
+}
+template <int HALF, int M>
+__device__ __forceinline__ void rs_level_pair(float* s, float* c, int lane) {
+  const bool hi = (lane & M) != 0;
+#pragma unroll
+  for (int i = 0; i < HALF; i++) {
+    const float ks = hi ? s[HALF + i] : s[i], kc = hi ? c[HALF + i] : c[i];
+    const float ss = hi ? s[i] : s[HALF + i], sc = hi ? c[i] : c[HALF + i];
+    const float rs = __shfl_xor_sync(0xffffffffu, ss, M), rc = __shfl_xor_sync(0xffffffffu, sc, M);
+    float t, e;
+    two_sum(ks, rs, t, e);
+    s[i] = t;
+    c[i] = kc + rc + e;
+  }
+}
+
 template <int MODE>
 struct Acc;
 template <>
 struct Acc<VS_REDUCE_FP32> {
-  float s[29];
+  float s[32];
   __device__ void zero() {
 #pragma unroll
-    for (int k = 0; k < 29; k++) s[k] = 0.0f;
+    for (int k = 0; k < 32; k++) s[k] = 0.0f;
   }
   __device__ void add(int k, float v) { s[k] += v; }
-  __device__ void begin_tree() {}
-  __device__ void shfl_add(unsigned m) {
-#pragma unroll
-    for (int k = 0; k < 29; k++) s[k] += __shfl_xor_sync(0xffffffffu, s[k], m);
+  // lane q < 29 returns the warp's sum of quantity q
+  __device__ float2 reduce_scatter(int lane) {
+    rs_level<16, 16>(s, lane);
+    rs_level<8, 8>(s, lane);
+    rs_level<4, 4>(s, lane);
+    rs_level<2, 2>(s, lane);
+    rs_level<1, 1>(s, lane);
+    return make_float2(s[0], 0.0f);
   }
-  __device__ float2 get(int k) const { return make_float2(s[k], 0.0f); }
 };
 template <>
 struct Acc<VS_REDUCE_KAHAN> {
-  float s[29], c[29];
+  float s[32];
   __device__ void zero() {
 #pragma unroll
-    for (int k = 0; k < 29; k++) s[k] = 0.0f;
+    for (int k = 0; k < 32; k++) s[k] = 0.0f;
   }
   __device__ void add(int k, float v) { s[k] += v; }
-  __device__ void begin_tree() {
+  __device__ float2 reduce_scatter(int lane) {
+    float c[16];
+    // first level: plain values in, (sum, error) pairs out
+    {
+      const bool hi = (lane & 16) != 0;
 #pragma unroll
-    for (int k = 0; k < 29; k++) c[k] = 0.0f;
-  }
-  __device__ void shfl_add(unsigned m) {
-#pragma unroll
-    for (int k = 0; k < 29; k++) {
-      float os = __shfl_xor_sync(0xffffffffu, s[k], m);
-      float oc = __shfl_xor_sync(0xffffffffu, c[k], m);
-      float t, e;
-      two_sum(s[k], os, t, e);
-      s[k] = t;
-      c[k] = c[k] + oc + e;
+      for (int i = 0; i < 16; i++) {
+        const float keep = hi ? s[16 + i] : s[i];
+        const float send = hi ? s[i] : s[16 + i];
+        float t, e;
+        two_sum(keep, __shfl_xor_sync(0xffffffffu, send, 16), t, e);
+        s[i] = t;
+        c[i] = e;
+      }
     }
+    rs_level_pair<8, 8>(s, c, lane);
+    rs_level_pair<4, 4>(s, c, lane);
+    rs_level_pair<2, 2>(s, c, lane);
+    rs_level_pair<1, 1>(s, c, lane);
+    return make_float2(s[0], c[0]);
   }
-  __device__ float2 get(int k) const { return make_float2(s[k], c[k]); }
 };
 template <>
 struct Acc<VS_REDUCE_FP64> {
-  double s[29];
+  double s[32];
   __device__ void zero() {
 #pragma unroll
-    for (int k = 0; k < 29; k++) s[k] = 0.0;
+    for (int k = 0; k < 32; k++) s[k] = 0.0;
   }
   __device__ void add(int k, float v) { s[k] += (double)v; }
-  __device__ void begin_tree() {}
-  __device__ void shfl_add(unsigned m) {
-#pragma unroll
-    for (int k = 0; k < 29; k++) s[k] += __shfl_xor_sync(0xffffffffu, s[k], m);
+  __device__ double2 reduce_scatter(int lane) {
+    rs_level<16, 16>(s, lane);
+    rs_level<8, 8>(s, lane);
+    rs_level<4, 4>(s, lane);
+    rs_level<2, 2>(s, lane);
+    rs_level<1, 1>(s, lane);
+    return make_double2(s[0], 0.0);
   }
-  __device__ double2 get(int k) const { return make_double2(s[k], 0.0); }
 };
 
 // Partial sums travel as (sum, error) pairs in the mode's own type: float2
@@ -509,13 +550,8 @@ __global__ void __launch_bounds__(kThreads, 3)
       acc.add(27, 1.0f);
       acc.add(28, b * b);
     }
-    acc.begin_tree();
-#pragma unroll
-    for (int m = 16; m >= 1; m >>= 1) acc.shfl_add(m);
-
-    if (lane == 0)
-#pragma unroll
-      for (int k = 0; k < 29; k++) wsum[warp][k] = acc.get(k);
+    const PT mine = acc.reduce_scatter(lane);
+    if (lane < 29) wsum[warp][lane] = mine;
     __syncthreads();
     PT* part = reinterpret_cast<PT*>(s->partials) + (size_t)vb * kPartials;
     if (threadIdx.x < 29) {
@@ -623,8 +659,12 @@ void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st) {
   k_gather_heads<<<kMaxSlots, 32, 0, st>>>(bt, reinterpret_cast<uint32_t*>(out));
 }
 
+#ifndef VS_ICP_PIXELS_PER_RANGE
+#define VS_ICP_PIXELS_PER_RANGE 512
+#endif
+
 int icp_blocks(int npix) {
-  int b = (npix + 511) / 512;
+  int b = (npix + VS_ICP_PIXELS_PER_RANGE - 1) / VS_ICP_PIXELS_PER_RANGE;
   if (b < 1) b = 1;
   if (b > kIcpMaxBlocks) b = kIcpMaxBlocks;
   return b;

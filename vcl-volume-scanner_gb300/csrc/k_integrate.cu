@@ -39,8 +39,15 @@ constexpr int kMaxImgLut = 2048;   // pixels per image axis
 // (z_yooji_cuda_volume_integrator.cu:133-135)
 __device__ inline int roundf_div8_ref(float x) { return (x < 0.0f) ? (int)(x - 0.5f) : (int)(x + 0.5f) / 8; }
 
+// 1 / w for every weight an update can produce (w = 1..65535), IEEE-rounded
+// exactly as the division it replaces
+__device__ float g_inv_weight[65536];
+
 // per-session tables: voxel centre coordinate per axis
-// (d_gpw_Get_Position_in_World) and the level-0 ray components K^-1 [x y 1]
+// (d_gpw_Get_Position_in_World), the level-0 ray components K^-1 [x y 1] and,
+// when kept, the per-pixel ray scale lambda^-1 = 1 / |K^-1 [x y 1]| of
+// g_ctvc (z_yooji_cuda_volume_integrator.cu:357-372), each with the
+// reference's own operations
 __global__ void k_session_tables(SessionDev* s) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const int d0 = s->dim[0], d1 = s->dim[1], d2 = s->dim[2];
@@ -48,8 +55,15 @@ __global__ void k_session_tables(SessionDev* s) {
   if (i < d1) s->lut_vox[d0 + i] = ((float)i + 0.5f) / s->vox_inv + s->origin[1];
   if (i < d2) s->lut_vox[d0 + d1 + i] = ((float)i + 0.5f) / s->vox_inv + s->origin[2];
   const float* K = s->lv[0].K;
-  if (i < s->lv[0].W) s->lut_ray[i] = 1.0f * ((float)i - K[2]) / K[0];
-  if (i < s->lv[0].H) s->lut_ray[s->lv[0].W + i] = 1.0f * ((float)i - K[3]) / K[1];
+  const int W = s->lv[0].W, H = s->lv[0].H;
+  if (i < W) s->lut_ray[i] = 1.0f * ((float)i - K[2]) / K[0];
+  if (i < H) s->lut_ray[W + i] = 1.0f * ((float)i - K[3]) / K[1];
+  if (i < 65536) g_inv_weight[i] = 1.0f / (float)i;
+  if (s->lam_map && i < W * H) {
+    const int x = i % W, y = i / W;
+    const float rx = 1.0f * ((float)x - K[2]) / K[0], ry = 1.0f * ((float)y - K[3]) / K[1];
+    s->lam_map[i] = 1.0f / sqrtf(rx * rx + ry * ry + 1.0f);
+  }
 }
 
 // frame counters of every slot
@@ -110,6 +124,7 @@ struct IntParams {
   const float* depth;
   const float* lut_vox;
   const float* lut_ray;
+  const float* lam_map;
   const uint32_t* list;
   uint32_t* flag;
   uint32_t* counters;
@@ -130,6 +145,7 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.depth = depth_ext ? depth_ext : s->depth_raw;
   q.lut_vox = s->lut_vox;
   q.lut_ray = s->lut_ray;
+  q.lam_map = s->lam_map;
   q.list = s->brick_list;
   q.flag = s->brick_flag;
   q.counters = s->brick_count;
@@ -160,8 +176,12 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.d1 = s->dim[1];
 }
 
+#ifndef VS_INT_MIN_BLOCKS
+#define VS_INT_MIN_BLOCKS 2  // resident 256-thread blocks per SM the register allocation must allow
+#endif
+
 template <class S>
-__global__ void __launch_bounds__(kIntThreads)
+__global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
     k_integrate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
                 const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext) {
   __shared__ uint32_t pre[kMaxSlots + 1];  // prefix of the slots' active-brick counts
@@ -186,6 +206,9 @@ __global__ void __launch_bounds__(kIntThreads)
   typedef typename S::word word;
   constexpr int kPerVec = 16 / sizeof(word);
   constexpr int kVecs = kBrickVox / kPerVec;  // 16-byte vectors per brick
+  constexpr int kLaneVec = kVecs / 32;        // vectors per lane
+  constexpr int kLaneVox = kLaneVec * kPerVec;  // 16 voxels per lane
+  constexpr int kRound = 8;
   const int lane = threadIdx.x & 31;
   const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -215,49 +238,84 @@ __global__ void __launch_bounds__(kIntThreads)
     const float* __restrict__ lz = q.lut_vox + q.d0 + q.d1;
     const float* __restrict__ rx_t = q.lut_ray;
     const float* __restrict__ ry_t = q.lut_ray + q.W;
-#pragma unroll 1
-    for (int k = 0; k < kVecs / 32; k++) {
-      const int vi = k * 32 + lane;
-      uint4 raw = bv[vi];
-      word wv[kPerVec];
-      memcpy(wv, &raw, 16);
-      bool changed = false;
+    // the lane's 16 voxels: all vector reads first, then two rounds of eight
+    // voxels whose depth (and ray-scale) gathers are in flight together
+    uint4 raw[kLaneVec];
 #pragma unroll
-      for (int e = 0; e < kPerVec; e++) {
-        const int li = vi * kPerVec + e;
+    for (int k = 0; k < kLaneVec; k++) raw[k] = bv[k * 32 + lane];
+    word wv[kLaneVec][kPerVec];
+#pragma unroll
+    for (int k = 0; k < kLaneVec; k++) memcpy(wv[k], &raw[k], 16);
+    bool changed[kLaneVec];
+#pragma unroll
+    for (int k = 0; k < kLaneVec; k++) changed[k] = false;
+#pragma unroll
+    for (int r = 0; r < kLaneVox / kRound; r++) {
+      int pix[kRound];
+      float dm[kRound], lam[kRound];
+#pragma unroll
+      for (int j = 0; j < kRound; j++) {
+        const int v = r * kRound + j, k = v / kPerVec, e = v % kPerVec;
+        const int li = (k * 32 + lane) * kPerVec + e;
         const int xc = bx * 8 + (li & 7), yc = by * 8 + ((li >> 3) & 7), zc = bz * 8 + (li >> 6);
         float told;
         uint32_t wold;
-        S::decode(wv[e], told, wold);
-        const float oldW = (float)wold;
-        if (oldW >= q.max_w) continue;
-        F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
-        F3 pc = transform(pg, q.T);
-        float u, v;
-        project(pc, q.K, u, v);
-        int x = __float2int_rn(u), y = __float2int_rn(v);
+        S::decode(wv[k][e], told, wold);
+        pix[j] = -1;
+        if ((float)wold >= q.max_w) continue;
+        const F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
+        const F3 pc = transform(pg, q.T);
+        float u, vv;
+        project(pc, q.K, u, vv);
+        const int x = __float2int_rn(u), y = __float2int_rn(vv);
         if (x < 0 || x > q.W - 1 || y < 0 || y > q.H - 1) continue;
-        float dm = __ldg(q.depth + (size_t)y * q.W + x);
-        if (!(dm > 0.0f)) continue;
-        float rx = __ldg(rx_t + x), ry = __ldg(ry_t + y);
-        float lam = 1.0f / sqrtf(rx * rx + ry * ry + 1.0f);
-        F3 dc = f3(pg.x - q.C[0], pg.y - q.C[1], pg.z - q.C[2]);
-        float nrm = sqrtf(dc.x * dc.x + dc.y * dc.y + dc.z * dc.z);
-        float sdf = dm - lam * nrm;
+        pix[j] = y * q.W + x;
+      }
+#pragma unroll
+      for (int j = 0; j < kRound; j++) {
+        dm[j] = 0.0f;
+        lam[j] = 0.0f;
+        if (pix[j] >= 0) {
+          dm[j] = __ldg(q.depth + pix[j]);
+          if (q.lam_map) lam[j] = __ldg(q.lam_map + pix[j]);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < kRound; j++) {
+        const int v = r * kRound + j, k = v / kPerVec, e = v % kPerVec;
+        if (pix[j] < 0 || !(dm[j] > 0.0f)) continue;
+        const int li = (k * 32 + lane) * kPerVec + e;
+        const int xc = bx * 8 + (li & 7), yc = by * 8 + ((li >> 3) & 7), zc = bz * 8 + (li >> 6);
+        float told;
+        uint32_t wold;
+        S::decode(wv[k][e], told, wold);
+        const float oldW = (float)wold;
+        float lm = lam[j];
+        if (!q.lam_map) {
+          const int x = pix[j] % q.W, y = pix[j] / q.W;
+          const float rx = __ldg(rx_t + x), ry = __ldg(ry_t + y);
+          lm = 1.0f / sqrtf(rx * rx + ry * ry + 1.0f);
+        }
+        const F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
+        const F3 dc = f3(pg.x - q.C[0], pg.y - q.C[1], pg.z - q.C[2]);
+        const float nrm = sqrtf(dc.x * dc.x + dc.y * dc.y + dc.z * dc.z);
+        const float sdf = dm[j] - lm * nrm;
         if (sdf < -q.mu) continue;
-        float ts = fminf(1.0f, sdf / q.mu);
-        float newW = oldW + 1.0f;
-        float inewW = 1.0f / newW;
-        float tnew = (oldW * told + ts) * inewW;
-        wv[e] = S::encode(tnew, (uint32_t)newW);
-        changed = true;
+        const float ts = fminf(1.0f, sdf / q.mu);
+        const float newW = oldW + 1.0f;
+        const float inewW = __ldg(g_inv_weight + (int)newW);
+        const float tnew = (oldW * told + ts) * inewW;
+        wv[k][e] = S::encode(tnew, (uint32_t)newW);
+        changed[k] = true;
         nupd++;
       }
-      if (changed) {
-        memcpy(&raw, wv, 16);
-        bv[vi] = raw;
-      }
     }
+#pragma unroll
+    for (int k = 0; k < kLaneVec; k++)
+      if (changed[k]) {
+        memcpy(&raw[k], wv[k], 16);
+        bv[k * 32 + lane] = raw[k];
+      }
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
     if (lane == 0) {
@@ -357,9 +415,22 @@ int sm_count() {
   return n;
 }
 
+template <class S>
+int resident_blocks() {
+  // one query per storage type (the answer depends only on the compiled kernel)
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_integrate<S>, kIntThreads, 0) != cudaSuccess || v < 1)
+      v = 1;
+    per_sm = v;
+  }
+  return sm_count() * per_sm;
+}
+
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) {
-  int m = h.dim[0];
-  for (int v : {h.dim[1], h.dim[2], h.lv[0].W, h.lv[0].H}) m = v > m ? v : m;
+  int m = 65536;
+  for (int v : {h.dim[0], h.dim[1], h.dim[2], h.lv[0].W * h.lv[0].H}) m = v > m ? v : m;
   k_session_tables<<<(m + 255) / 256, 256, 0, st>>>(d);
 }
 
@@ -367,17 +438,16 @@ void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, c
                       bool gate, cudaStream_t st) {
   k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt);
   k_activate<<<sm_count() * 8, dim3(32, 8), 0, st>>>(bt, depth, Tcg, gate ? 1 : 0);
-  // persistent grid: enough warps to cover every SM several times over
-  const int blocks = sm_count() * 4;
+  // persistent grid: every block resident at once
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      k_integrate<StoreF16><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      k_integrate<StoreF16><<<resident_blocks<StoreF16>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
     case VS_TSDF_FP32:
-      k_integrate<StoreF32><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      k_integrate<StoreF32><<<resident_blocks<StoreF32>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
     default:
-      k_integrate<StoreI16><<<blocks, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      k_integrate<StoreI16><<<resident_blocks<StoreI16>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
       break;
   }
 }

@@ -277,6 +277,7 @@ size_t vs_session_bytes(const vs_config* c) {
   b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + sizeof(BatchTable) + 64;
   b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
   for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
+  b += (size_t)w * h * 4;                                                      // ray-scale map
   return b;
 }
 
@@ -338,6 +339,7 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.pose, sizeof(Pose));
   rc |= alloc(s, &h.lut_vox, (size_t)(h.dim[0] + h.dim[1] + h.dim[2]) * 4);
   rc |= alloc(s, &h.lut_ray, (size_t)(h.lv[0].W + h.lv[0].H) * 4);
+  rc |= alloc(s, &h.lam_map, n0 * 4);
   {
     size_t npx = 0;
     for (int l = 0; l < h.levels; l++) npx += (size_t)h.lv[l].W * h.lv[l].H;

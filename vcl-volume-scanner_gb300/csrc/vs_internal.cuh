@@ -93,6 +93,7 @@ struct SessionDev {
   float* lut_vox;                // voxel centre coordinate per axis: dim[0] + dim[1] + dim[2]
   float* lut_ray;                // level-0 K^-1 [x 1 1] (W) then [1 y 1] (H) components
   float4* ray_hit;               // ray-cast surface points, every level's pixels in turn
+  float* lam_map;                // level-0 ray scale per pixel (NULL: computed per voxel)
 };
 
 // Sessions advanced together by one launch of every per-frame kernel.  The
