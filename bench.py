@@ -158,17 +158,22 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel_key):
-    """DRAM bytes per launch of a kernel from the committed ncu summary."""
+def traffic_per_unit(kernel_key, unit_key):
+    """DRAM bytes per unit of work of a kernel, from the committed ncu summary
+    (profiles/ncu_traffic.txt: `kernel key value ...`)"""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
     try:
         for line in open(p):
             parts = line.split()
-            if len(parts) >= 3 and parts[0] == kernel_key and parts[1] == "dram_bytes_per_launch":
+            if len(parts) >= 3 and parts[0] == kernel_key and parts[1] == unit_key:
                 return float(parts[2])
-    except OSError:
+    except (OSError, ValueError):
         pass
     return None
+
+
+def level_pixels(cfg):
+    return [(cfg.width >> l) * (cfg.height >> l) for l in range(cfg.levels)]
 
 
 class ClockSampler:
@@ -469,14 +474,32 @@ def run_ours(args):
     dom_i = int(np.argmax(stage_sum))
     dom = names[dom_i]
     achieved = {k: alg[k] / (stage_sum[names.index(k)] * 1e-3) / 1e9 for k in names}
-    kernel_key = {"integrate": "k_integrate", "raycast": "k_raycast", "track": "k_icp_iter",
+    kernel_key = {"integrate": "k_integrate", "raycast": "k_ray_march+k_ray_shade", "track": "k_icp_iter",
                   "filter": "k_bilateral_batch"}[dom]
-    roofline = {"bound": "hbm", "kernel": kernel_key, "stage": dom, "achieved": achieved[dom], "peak": peak,
-                "unit": "GB/s", "frac": achieved[dom] / peak, "traffic": traffic_from_profiles(kernel_key),
+    # measured DRAM bytes of one step of the stage: per-unit figures of the
+    # committed ncu captures times this workload's units per step
+    rays = np.mean([sum(sum(level_pixels(seqs[i]["cfg"])) for i in members[r]) for r in range(n_stage)])
+    traffic = None
+    if dom == "raycast":
+        a_, b_ = traffic_per_unit("k_ray_march", "dram_bytes_per_ray"), traffic_per_unit("k_ray_shade",
+                                                                                          "dram_bytes_per_ray")
+        if a_ is not None and b_ is not None:
+            traffic = (a_ + b_) * rays
+    elif dom == "track":
+        px = traffic_per_unit("k_icp_iter", "dram_bytes_per_pixel")
+        if px is not None:
+            traffic = px * np.mean([sum(sum(p * it for p, it in zip(level_pixels(seqs[i]["cfg"]), MIX["icp_iters"]))
+                                        for i in members[r]) for r in range(n_stage)])
+    roofline = {"bound": "hbm", "kernel": kernel_key, "stage": dom,
+                "achieved": achieved[dom], "peak": peak, "unit": "GB/s", "frac": achieved[dom] / peak,
+                "traffic": traffic,
+                "traffic_note": "DRAM bytes per step: bytes per unit from profiles/ncu_traffic.txt x units per step "
+                                "(%.0f rays)" % rays,
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6800 GB/s",
-                "note": "algorithmic bytes of the stage over the sessions of %d full steps / its event-timed "
-                        "duration" % n_stage,
+                "note": "algorithmic bytes of the stage per full step (the sessions of the first %d steps) / its "
+                        "event-timed duration; the ray-cast is issue-bound, not HBM-bound (see profiles/)" % n_stage,
+                "algorithmic_bytes_per_step": alg[dom] / n_stage,
                 "stages_gbs": achieved, "stages_frac": {k: v / peak for k, v in achieved.items()}}
 
     cpu = None

@@ -68,16 +68,22 @@ struct Vol {
   // occupancy cell - so that the march only has to advance the position for
   // them.  The bounds are pulled in by 0.05 voxel, far more than the
   // rounding of the position accumulated over a run (at most 64 steps of
-  // float additions, under 1e-2 voxel for coordinates below 2048).
+  // float additions, under 1e-2 voxel for coordinates below 2048) or of the
+  // approximate reciprocals of the increment.  A negative result -k says the
+  // position lies in an occupied 32^3 cell that the ray leaves after about k
+  // steps; the caller need not ask again before then (asking late only
+  // delays a run, it never changes a sample).
   __device__ inline int free_run(F3 p, F3 inc) const {
     if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return 0;
     const float d = 0.05f;
     const float pa[3] = {p.x, p.y, p.z}, ia[3] = {inc.x, inc.y, inc.z};
+    const float ra[3] = {__fdividef(1.0f, inc.x), __fdividef(1.0f, inc.y), __fdividef(1.0f, inc.z)};
     // a coordinate is in range iff -0.5 < p < dim - 0.5 (gtvu rounds with ROUNDF)
     bool inside = true;
 #pragma unroll
     for (int a = 0; a < 3; a++) inside &= pa[a] > -0.5f && pa[a] < (float)dim[a] - 0.5f;
     float t;
+    bool occupied_cell = false;
     if (!inside) {
       // outside until every coordinate that is out of range has come in
       t = 0.0f;
@@ -85,35 +91,35 @@ struct Vol {
       for (int a = 0; a < 3; a++) {
         const float hi = (float)dim[a] - 0.5f;
         if (pa[a] <= -0.5f)
-          t = fmaxf(t, ia[a] > 0.0f ? (-0.5f - d - pa[a]) / ia[a] : 1e30f);
+          t = fmaxf(t, ia[a] > 0.0f ? (-0.5f - d - pa[a]) * ra[a] : 1e30f);
         else if (pa[a] >= hi)
-          t = fmaxf(t, ia[a] < 0.0f ? (hi + d - pa[a]) / ia[a] : 1e30f);
+          t = fmaxf(t, ia[a] < 0.0f ? (hi + d - pa[a]) * ra[a] : 1e30f);
       }
     } else {
       const int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
-      int size;
+      int size = 32;
       if (!cell_set(occ2, nc2, 7, x, y, z))
         size = 128;
-      else if (!cell_set(occ1, nc1, 5, x, y, z))
-        size = 32;
-      else
-        return 0;
+      else if (cell_set(occ1, nc1, 5, x, y, z))
+        occupied_cell = true;
       const int c[3] = {x & ~(size - 1), y & ~(size - 1), z & ~(size - 1)};
       t = 1e30f;
 #pragma unroll
       for (int a = 0; a < 3; a++) {
         const float lo = (float)c[a] - 0.5f, hi = lo + (float)size;
         if (ia[a] > 0.0f)
-          t = fminf(t, (hi - d - pa[a]) / ia[a]);
+          t = fminf(t, (hi - d - pa[a]) * ra[a]);
         else if (ia[a] < 0.0f)
-          t = fminf(t, (lo + d - pa[a]) / ia[a]);
+          t = fminf(t, (lo + d - pa[a]) * ra[a]);
       }
     }
     // steps k >= 1 with k < t
     t = fminf(t, 65.0f);
     const int m = (int)ceilf(t) - 1;
+    if (occupied_cell) return m > 0 ? -m : 0;
     return m > 0 ? m : 0;
   }
+
   __device__ inline bool occupied(int x, int y, int z) const {
     const uint32_t b = ((uint32_t)(z >> 3) * (uint32_t)nb[1] + (uint32_t)(y >> 3)) * (uint32_t)nb[0] + (uint32_t)(x >> 3);
     return (__ldg(occ + (b >> 5)) >> (b & 31)) & 1u;
@@ -269,6 +275,7 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
     return false;
   const int cap = 4 * (int)total_max + 64;
   int it = 0;
+  int recheck = 0;  // full steps before the next free-space test
   while (state != BEHIND) {
     if (++it > cap) return false;
     if (state == COARSE)
@@ -291,18 +298,28 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
         state = FINE;
       }
     }
-    if (tsdf == 1.0f && state != BEHIND) {
+    if (tsdf == 1.0f && state != BEHIND && --recheck < 0) {
       // While samples read "no value" (TSDF 1) the state and the step stay as
       // they are, so the steps of a free-space run are replayed with the same
       // float operations as the loop above, without the volume reads.
       const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
       const F3 inc = scale(sn, rd);
-      for (int m = V.free_run(vs, inc); m > 0; m--) {
-        if (++it > cap) return false;
+      int m = V.free_run(vs, inc);
+      if (m < 0) {
+        recheck = -m;
+        m = 0;
+      }
+      // the loop above would stop at iteration cap + 1: run at most cap - it
+      // steps here, then stop as it would
+      const bool capped = m > cap - it;
+      const int run = capped ? cap - it : m;
+      for (int k = 0; k < run; k++) {
         vs = add(vs, inc);
         total += sn;
         if (total > total_max) return false;
       }
+      it += run;
+      if (capped) return false;
     }
   }
   if (state == BEHIND) {
