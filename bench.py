@@ -63,7 +63,11 @@ MIX = dict(name="serving_mix_64", sessions=64, seed=5, length=(50, 500),
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500, help="batched steps (frames per session are capped at it)")
+    ap.add_argument("--steps", type=int, default=None,
+                    help="serving mix: batched steps (session lengths are capped at it, default 500); "
+                         "plain_vga: timed frames (default 295); precision: frames (default 30)")
+    ap.add_argument("--workload", default="serving_mix", choices=["serving_mix", "plain_vga"])
+    ap.add_argument("--study", default=None, choices=["precision"])
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sessions", type=int, default=MIX["sessions"])
@@ -72,7 +76,11 @@ def parse():
     ap.add_argument("--ate-frames", type=int, default=12)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    return ap.parse_args()
+    ap.add_argument("--no-autotune", action="store_true")
+    a = ap.parse_args()
+    if a.steps is None:
+        a.steps = 30 if a.study == "precision" else (295 if a.workload == "plain_vga" else 500)
+    return a
 
 
 def dist_env():
@@ -226,6 +234,31 @@ class ClockSampler:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def max_over_ranks(value, world):
+    """the largest value over the ranks of the job (gloo on CPU tensors, NCCL
+    on the current CUDA device)"""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier_all(world):
+    import torch
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
 def pct(a, q):
     return float(np.percentile(np.asarray(a, np.float64), q)) if len(a) else None
 
@@ -334,11 +367,7 @@ def run_ours(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-
-            dist.barrier()
-        torch.cuda.synchronize()
+        barrier_all(world)
 
     t_gen = time.perf_counter()
     seqs = build_workload(args.sessions, args.steps, MIX["seed"])
@@ -356,11 +385,17 @@ def run_ours(args):
     batch = V.Batch()
 
     # ---- warm-up: graph capture and first launches on throwaway sessions ----
-    warm = [V.Session(seqs[i]["cfg"]) for i in range(min(4, n_s))]
+    n_warm = min(16, n_s)
+    warm = [V.Session(seqs[i]["cfg"]) for i in range(n_warm)]
     for k in range(args.warmup):
-        batch.step(warm, [frames_dev[i][min(k, lens[i] - 1)].data_ptr() for i in range(len(warm))],
-                   st.cuda_stream)
+        batch.step(warm, [frames_dev[i][min(k, lens[i] - 1)].data_ptr() for i in range(n_warm)], st.cuda_stream)
     batch.sync()
+    # autotuner: the ray-cast launch shape, timed on the warm-up sessions
+    tuned = None
+    if not args.no_autotune:
+        shape, ms = batch.autotune(warm, reps=3)
+        tuned = {"ray_tile": "%dx%d" % (1 << shape[0], 32 >> shape[0]), "march_blocks_per_sm": shape[1],
+                 "shade_blocks_per_sm": shape[2], "raycast_ms_warm_sessions": ms}
     for w in warm:
         w.close()
 
@@ -382,13 +417,7 @@ def run_ours(args):
     barrier()
     clocks = clk.stop()
     step_ms = np.array([ev[r].elapsed_time(ev[r + 1]) for r in range(rounds)])
-    total_ms = float(ev[0].elapsed_time(ev[rounds]))
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = max_over_ranks(float(ev[0].elapsed_time(ev[rounds])), world)
     fps_batched = world * n_frames / (total_ms / 1000.0)
     kps = batch.kernels_per_step()
     tracked_batched = [int(s.pose()[2][0]) for s in sessions]
@@ -426,13 +455,7 @@ def run_ours(args):
         for j, i in enumerate(members[r]):
             if i in e2e_poses and len(e2e_poses[i]) < args.ate_frames:
                 e2e_poses[i].append(T[j].astype(np.float64))
-    e2e_s = time.perf_counter() - t0
-    if world > 1:
-        import torch.distributed as dist
-
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     fps_e2e = world * n_frames / e2e_s
     h2d = int(round(sum(h.nbytes for h in host) / rounds))  # mean host frame bytes per step
     d2h = 64 * 80  # pose heads of every slot, one copy per step
@@ -450,7 +473,7 @@ def run_ours(args):
                 sessions[i].scan_frame(frames_dev[i][r].data_ptr(), st.cuda_stream)
     pev[1].record(st)
     st.synchronize()
-    plain_ms = float(pev[0].elapsed_time(pev[1]))
+    plain_ms = max_over_ranks(float(pev[0].elapsed_time(pev[1])), world)
     fps_plain = world * n_frames / (plain_ms / 1000.0)
     # the batched and plain runs of every session end on the same FP64 pose
     plain_equal = all(np.array_equal(sessions[i].pose()[1], final_batched[i]) for i in range(n_s))
@@ -525,6 +548,7 @@ def run_ours(args):
             "e2e": {"value": fps_e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "note": "vs_batch_step_host per step: pinned host frames in, pose heads out"},
             "gpu_launches": int(kps * rounds),
+            "autotune": tuned,
             "clocks": clocks,
             "ate": ate,
             "tracked_last_frame": int(sum(tracked_batched)),
@@ -645,9 +669,306 @@ def ate_vs_fp64(seqs, poses, nf):
     return {"vs_fp64_oracle_mm": worst, "sessions": out}
 
 
+# ---------------------------------------------------------------------------
+# --workload plain_vga: one session, 640x480, 512^3
+# ---------------------------------------------------------------------------
+VGA = dict(name="plain_vga_512", width=640, height=480, fx=525.0, fy=525.0, cx=319.5, cy=239.5, volume=512,
+           size_m=1.5, mu=0.02, icp_iters=(10, 5, 4), th_icp=0.1 ** 2, normal_deg=20.0, dropout_blob=0.015,
+           max_depth=2.5, seed=2)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def vga_frames(n):
+    import vs_scanner as V
+
+    w = VGA
+    sc = V.synth_config(w["width"], w["height"], fx=w["fx"], fy=w["fy"], cx=w["cx"], cy=w["cy"], n_frames=n,
+                        seed=w["seed"], dropout_blob=w["dropout_blob"], max_depth=w["max_depth"])
+    return V.synth_generate(sc)
+
+
+def vga_config(centre):
+    import vs_scanner as V
+
+    w = VGA
+    origin, vox = V.cube_around(centre, w["size_m"], w["volume"])
+    return V.default_config(w["width"], w["height"], fx=w["fx"], fy=w["fy"], cx=w["cx"], cy=w["cy"],
+                            dim=(w["volume"],) * 3, origin=origin, voxel_size=vox, mu=w["mu"], th_icp=w["th_icp"],
+                            cos_normal=float(np.cos(np.radians(w["normal_deg"]))), icp_iters=w["icp_iters"],
+                            tsdf_type=V.VS_TSDF_INT16, reduce_mode=V.VS_REDUCE_KAHAN)
+
+
+def vga_config_json(args, world):
+    w = VGA
+    return {"workload": "%s: 1 session, %dx%d uint16 depth, %d^3 int16+uint16 TSDF over %.1f m, mu %.0f cm, "
+                        "ICP %d/%d/%d, 10 cm / 20 deg rejection" % (
+                            w["name"], w["width"], w["height"], w["volume"], w["size_m"], w["mu"] * 100,
+                            *w["icp_iters"]),
+            "frames": args.steps, "sessions_per_gpu": 1, "parallelism": "replicas x%d" % world,
+            "l2": "flushed between frames (256 MB write outside the timed events)",
+            "scene": "seeded synthetic spheres/boxes on a ground plane, orbit 0.9 m, seed %d" % w["seed"]}
+
+
+def run_plain_vga_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    import oracle_py as O
+
+    n_threads = os.cpu_count() or 1
+    O.load()
+    set_omp_threads(n_threads)
+    warm = min(args.warmup, 3)
+    depth, gt, centre = vga_frames(warm + args.steps)
+    s = O.Session(O.config_from_vs(vga_config(centre), reduce_mode=0))
+    for k in range(warm):
+        s.frame(depth[k])
+    times = []
+    t_start = time.perf_counter()
+    for k in range(warm, warm + args.steps):
+        t0 = time.perf_counter()
+        s.frame(depth[k])
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_start > args.ref_seconds:
+            break
+    total = sum(times)
+    fps = len(times) / total
+    sample = "%d frames of the VGA sequence after %d warm-up frames, oracle port (reference FP32 semantics), " \
+             "%d threads" % (len(times), warm, n_threads)
+    print(json.dumps({"impl": "reference", "metric": "frames/s", "value": fps, "unit": "frames/s",
+                      "n_gpus": args.gpus, "steps": len(times), "warmup": warm, "ms_per_step": 1000.0 * total / len(times),
+                      "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                      "data": "synthetic", "config": vga_config_json(args, 1),
+                      "cpu_baseline": {"value": fps, "unit": "frames/s", "cores": n_threads, "kind": "port",
+                                       "sample": sample},
+                      "e2e": {"value": fps, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}),
+          flush=True)
+
+
+def run_plain_vga(args):
+    import torch
+
+    import vs_scanner as V
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    depth, gt, centre = vga_frames(args.warmup + args.steps)
+    cfg = vga_config(centre)
+    frames_dev = torch.from_numpy(depth.view(np.int16)).cuda()
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    st = torch.cuda.Stream()
+    sess = V.Session(cfg)
+    sess.set_stage_timing(True)
+    with torch.cuda.stream(st):
+        for k in range(args.warmup):
+            flush.zero_()
+            sess.scan_frame(frames_dev[k].data_ptr(), st.cuda_stream)
+    st.synchronize()
+    clk = ClockSampler(local)
+    barrier_all(world)
+    clk.start()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    stage = np.zeros((args.steps, 4))
+    stats = np.zeros((args.steps, 4))
+    with torch.cuda.stream(st):
+        for i in range(args.steps):
+            flush.zero_()
+            ev[i][0].record(st)
+            sess.scan_frame(frames_dev[args.warmup + i].data_ptr(), st.cuda_stream)
+            ev[i][1].record(st)
+            stage[i] = sess.stage_times()
+            stats[i] = sess.frame_stats()
+    st.synchronize()
+    barrier_all(world)
+    clocks = clk.stop()
+    frame_ms = np.array([a.elapsed_time(b) for a, b in ev])
+    total_ms = max_over_ranks(float(frame_ms.sum()), world)
+    fps = world * args.steps / (total_ms / 1000.0)
+    kpf = sess.kernels_per_frame()
+    # end to end: host frames through vs_scan_frame_host
+    sess.set_stage_timing(False)
+    sess.reset()
+    host = torch.from_numpy(depth.view(np.int16)).pin_memory().numpy().view(np.uint16)
+    for k in range(args.warmup):
+        flush.zero_()
+        torch.cuda.synchronize()
+        sess.scan_frame_host(host[k])
+    e2e_t, poses = [], []
+    for i in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        T, _ = sess.scan_frame_host(host[args.warmup + i])
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_fps = world * args.steps / max_over_ranks(sum(e2e_t), world)
+    sess.close()
+    if rank != 0:
+        return
+    names = ["filter", "track", "integrate", "raycast"]
+    stage_mean = stage.mean(axis=0)
+    peak, peak_kind = measured_peak_hbm()
+    st_ = (stats[:, 0].mean(), stats[:, 1].mean())
+    alg = stage_bytes(cfg, st_)
+    dom = names[int(np.argmax(stage_mean))]
+    achieved = {k: alg[k] / (stage_mean[names.index(k)] * 1e-3) / 1e9 for k in names}
+    rays = sum(level_pixels(cfg))
+    traffic = None
+    if dom == "raycast":
+        a_, b_ = traffic_per_unit("k_ray_march", "dram_bytes_per_ray"), traffic_per_unit("k_ray_shade",
+                                                                                          "dram_bytes_per_ray")
+        if a_ is not None and b_ is not None:
+            traffic = (a_ + b_) * rays
+    elif dom == "track":
+        px = traffic_per_unit("k_icp_iter", "dram_bytes_per_pixel")
+        if px is not None:
+            traffic = px * sum(p * it for p, it in zip(level_pixels(cfg), VGA["icp_iters"]))
+    cpu = ate = None
+    if not args.no_cpu:
+        import oracle_py as O
+
+        O.load()
+        set_omp_threads(1)
+        s = O.Session(O.config_from_vs(cfg, reduce_mode=0))
+        n, t0 = 0, time.perf_counter()
+        while n < depth.shape[0] and (time.perf_counter() - t0 < args.cpu_seconds or n < 2):
+            s.frame(depth[n])
+            n += 1
+        dt = time.perf_counter() - t0
+        cpu = {"value": n / dt, "unit": "frames/s", "cores": 1, "kind": "port",
+               "sample": "first %d frames of the sequence (%.1f s), oracle port, reference FP32 semantics, 1 thread"
+                         % (n, dt)}
+        nf = min(n, args.ate_frames)
+        set_omp_threads(os.cpu_count() or 1)
+        s64 = O.Session(O.config_from_vs(cfg, reduce_mode=3, tsdf_store=0), f64=True)
+        s2 = V.Session(cfg)
+        ours, ref = [], []
+        for k in range(nf):
+            T, _ = s2.scan_frame_host(host[k])
+            ours.append(T.astype(np.float64))
+            s64.frame(depth[k])
+            ref.append(s64.pose_f64())
+        s2.close()
+        d = np.linalg.norm(centres(ours) - centres(ref), axis=1)
+        ate = {"vs_fp64_oracle_mm": float(np.sqrt(np.mean(d ** 2)) * 1e3), "frames": nf,
+               "max_mm": float(d.max() * 1e3)}
+    line = {"metric": "frames/s", "value": fps, "unit": "frames/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": float(frame_ms.mean()), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": vga_config_json(args, world),
+            "latency_ms": {"p50": pct(frame_ms, 50), "p99": pct(frame_ms, 99), "max": float(frame_ms.max())},
+            "stages_ms": {n_: float(v) for n_, v in zip(names, stage_mean)},
+            "roofline": {"bound": "hbm", "kernel": {"raycast": "k_ray_march+k_ray_shade", "track": "k_icp_iter",
+                                                    "integrate": "k_integrate", "filter": "k_bilateral_batch"}[dom],
+                         "stage": dom, "achieved": achieved[dom], "peak": peak, "unit": "GB/s",
+                         "frac": achieved[dom] / peak, "traffic": traffic,
+                         "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
+                         "fallback 6800 GB/s", "stages_gbs": achieved},
+            "integrate": {"active_subcubes": st_[0], "voxels_updated": st_[1],
+                          "achieved_gbs": achieved["integrate"], "frac": achieved["integrate"] / peak},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_fps, "unit": "frames/s", "h2d_bytes_per_step": cfg.width * cfg.height * 2,
+                    "d2h_bytes_per_step": 80},
+            "gpu_launches": int(kpf * args.steps), "clocks": clocks, "ate": ate}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# --study precision: reductions x TSDF storage against the FP64 oracle
+# ---------------------------------------------------------------------------
+def run_precision(args):
+    """Configuration-1 workload (one 320x240 session, fx = fy = 285, cx = 160,
+    cy = 120, 1 % dropout, ICP 10/5/4, mu 3 cm) with the TSDF in a 512^3 volume
+    over 1 m.  Every reduction mode x every TSDF storage runs on the GPU; the
+    FP64 oracle (double arithmetic, FP64 sums, double TSDF) runs the same
+    frames on the CPU.  Errors: per-frame pose against the FP64 oracle's pose
+    of the same frame, ATE against the FP64 trajectory and the generator's
+    ground truth, final TSDF and level-0 model maps against the oracle's."""
+    import oracle_py as O
+    import vs_scanner as V
+
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    nf = args.steps
+    sc = V.synth_config(320, 240, fx=285.0, fy=285.0, cx=160.0, cy=120.0, n_frames=nf, seed=1, dropout_iid=0.01)
+    depth, gt, centre = V.synth_generate(sc)
+    origin, vox = V.cube_around(centre, 1.0, 512)
+
+    def cfg_of(reduce_mode, tsdf_type):
+        return V.default_config(320, 240, fx=285.0, fy=285.0, cx=160.0, cy=120.0, dim=(512,) * 3, origin=origin,
+                                voxel_size=vox, mu=0.03, th_icp=0.1 ** 2, icp_iters=(10, 5, 4),
+                                tsdf_type=tsdf_type, reduce_mode=reduce_mode)
+
+    O.load()
+    set_omp_threads(os.cpu_count() or 1)
+    t0 = time.perf_counter()
+    ref = O.Session(O.config_from_vs(cfg_of(V.VS_REDUCE_FP64, V.VS_TSDF_FP32), reduce_mode=3, tsdf_store=0), f64=True)
+    ref_poses = []
+    for k in range(nf):
+        ref.frame(depth[k])
+        ref_poses.append(ref.pose_f64())
+    ref_t, ref_w = ref.volume().get()
+    ref_maps = ref.maps(0)
+    t_oracle = time.perf_counter() - t0
+    gt_c = centres([np.asarray(g) for g in gt])
+
+    def ate(a, b):
+        d = np.linalg.norm(centres(a) - centres(b), axis=1)
+        return float(np.sqrt(np.mean(d ** 2)) * 1e3)
+
+    rows = []
+    for rm, rname in ((V.VS_REDUCE_FP32, "fp32"), (V.VS_REDUCE_KAHAN, "two-sum fp32"), (V.VS_REDUCE_FP64, "fp64")):
+        for tt, tname in ((V.VS_TSDF_INT16, "int16"), (V.VS_TSDF_FP16, "fp16"), (V.VS_TSDF_FP32, "fp32")):
+            s = V.Session(cfg_of(rm, tt))
+            poses = []
+            for k in range(nf):
+                s.scan_frame_host(depth[k])
+                poses.append(s.pose()[1])
+            t, w = s.volume()
+            m = s.maps(0)
+            s.close()
+            rot = [float(np.arctan2(np.linalg.norm([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / 2,
+                                    (np.trace(R) - 1) / 2))
+                   for R in (np.asarray(a)[:3, :3].T @ np.asarray(b)[:3, :3] for a, b in zip(poses, ref_poses))]
+            trans = [float(np.linalg.norm(np.asarray(a)[:3, 3] - np.asarray(b)[:3, 3]) * 1e3)
+                     for a, b in zip(poses, ref_poses)]
+            both = (w > 0) & (ref_w > 0)
+            dt_ = np.abs(t[both].astype(np.float64) - ref_t[both].astype(np.float64))
+            va = m["model_vertex"].reshape(-1, 3)
+            vb = ref_maps["model_vertex"].reshape(-1, 3)
+            valid = (va[:, 0] != -100.0) & (vb[:, 0] != -100.0)
+            dv = np.linalg.norm(va[valid] - vb[valid], axis=1) * 1e3
+            rows.append({"reduction": rname, "tsdf": tname,
+                         "pose_rot_max_rad": max(rot), "pose_trans_max_mm": max(trans),
+                         "ate_vs_fp64_mm": ate(poses, ref_poses),
+                         "ate_vs_ground_truth_mm": float(np.sqrt(np.mean(np.linalg.norm(
+                             centres(poses) - gt_c, axis=1) ** 2)) * 1e3),
+                         "tsdf_abs_err_mean": float(dt_.mean()) if dt_.size else None,
+                         "tsdf_abs_err_max": float(dt_.max()) if dt_.size else None,
+                         "weight_mismatch_voxels": int(np.count_nonzero(w != ref_w)),
+                         "raycast_vertex_err_mean_mm": float(dv.mean()) if dv.size else None,
+                         "raycast_within_1mm": float(np.mean(dv < 1.0)) if dv.size else None,
+                         "raycast_valid_agree": float(np.mean((va[:, 0] != -100.0) == (vb[:, 0] != -100.0)))})
+    out = {"study": "precision", "workload": "config 1: 320x240, %d frames, fx=fy=285, 512^3 over 1 m, mu 3 cm, "
+                                             "ICP 10/5/4" % nf,
+           "reference": "FP64 oracle (double arithmetic, FP64 sums, double TSDF) on the host, %.1f s" % t_oracle,
+           "fp64_oracle_ate_vs_ground_truth_mm": float(np.sqrt(np.mean(np.linalg.norm(
+               centres(ref_poses) - gt_c, axis=1) ** 2)) * 1e3),
+           "variants": rows}
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.study == "precision":
+        run_precision(args)
+    elif args.workload == "plain_vga":
+        (run_plain_vga_reference if args.impl == "reference" else run_plain_vga)(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

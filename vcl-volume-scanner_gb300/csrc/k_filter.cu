@@ -376,10 +376,12 @@ void configure_filter_kernels() {
 
 // work-item prefixes of a batch; host_recs are the host copies of the
 // session records, dev_recs their device addresses
-void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs,
-                      int n) {
+void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n,
+                      int ray_lx) {
   std::memset(&hb, 0, sizeof(hb));
   hb.n = n;
+  hb.ray_lx = ray_lx;
+  const int rx = 1 << ray_lx, ry = 32 >> ray_lx;
   for (int i = 0; i < n; i++) {
     const SessionDev& h = *host_recs[i];
     hb.s[i] = dev_recs[i];
@@ -389,7 +391,7 @@ void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const 
       const int w = h.lv[l].W, hh = h.lv[l].H;
       ipre += ((w + 31) / 32) * ((hh + 7) / 8);
       ipost += ((w + 15) / 16) * ((hh + 15) / 16);
-      ray += ((w + 7) / 8) * ((hh + 3) / 4);
+      ray += ((w + rx - 1) / rx) * ((hh + ry - 1) / ry);
     }
     hb.bil[i + 1] = hb.bil[i] + ((h.lv[0].W + BX - 1) / BX) * ((h.lv[0].H + BY - 1) / BY);
     for (int l = 1; l < kMaxLevels; l++)

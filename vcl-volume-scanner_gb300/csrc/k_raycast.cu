@@ -26,8 +26,7 @@
 namespace vs {
 namespace {
 
-constexpr int RX = 8, RY = 4;      // the 32 rays of one warp's tile
-constexpr int kRayThreads = 128;
+constexpr int kRayThreads = 128;  // a warp's 32 rays form a (1 << lx) x (32 >> lx) tile
 
 struct RayArgs {
   const BatchTable* bt;
@@ -334,11 +333,11 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
   return false;
 }
 
-__device__ inline int ray_tiles(const SessionDev& s, int l) {
-  return ((s.lv[l].W + RX - 1) / RX) * ((s.lv[l].H + RY - 1) / RY);
+__device__ inline int ray_tiles(const SessionDev& s, int l, int rx, int ry) {
+  return ((s.lv[l].W + rx - 1) / rx) * ((s.lv[l].H + ry - 1) / ry);
 }
 
-// Hands the calling warp 8x4-ray tiles until none are left and calls
+// Hands the calling warp ray tiles until none are left and calls
 // f(session, level, x, y) for each lane's pixel inside its level.  The last
 // warp to finish clears the counters for the next launch.
 template <class F>
@@ -346,7 +345,8 @@ __device__ inline void for_each_ray_tile(const RayArgs& a, F&& f) {
   const BatchTable* __restrict__ bt = a.bt;
   const int lane = threadIdx.x & 31;
   const int n = bt->n;
-  const int total = (a.level >= 0) ? ray_tiles(*bt->s[0], a.level) : bt->ray[n];
+  const int lx = bt->ray_lx, rx = 1 << lx, ry = 32 >> lx;
+  const int total = (a.level >= 0) ? ray_tiles(*bt->s[0], a.level, rx, ry) : bt->ray[n];
   for (;;) {
     int item = 0;
     if (lane == 0) item = (int)atomicAdd(a.work, 1u);
@@ -362,15 +362,15 @@ __device__ inline void for_each_ray_tile(const RayArgs& a, F&& f) {
       const SessionDev& s = *bt->s[slot];
       l = 0;
       for (; l < s.levels - 1; l++) {
-        const int nt = ray_tiles(s, l);
+        const int nt = ray_tiles(s, l, rx, ry);
         if (t < nt) break;
         t -= nt;
       }
     }
     const SessionDev& s = *bt->s[slot];
     if (a.gate && s.pose->failed) continue;
-    const int tw = (s.lv[l].W + RX - 1) / RX;
-    const int x = (t % tw) * RX + (lane & (RX - 1)), y = (t / tw) * RY + (lane / RX);
+    const int tw = (s.lv[l].W + rx - 1) / rx;
+    const int x = (t % tw) * rx + (lane & (rx - 1)), y = (t / tw) * ry + (lane >> lx);
     if (x < s.lv[l].W && y < s.lv[l].H) f(s, l, x, y);
   }
   if (lane == 0) {
@@ -508,26 +508,33 @@ __global__ void k_maps_export(const float4* __restrict__ mv, const float4* __res
 }  // namespace
 
 template <class K>
-int resident_grid(K kernel) {
+int max_per_sm(K kernel) {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kRayThreads, 0) != cudaSuccess || per_sm < 1)
     per_sm = 4;
-  return sm_count() * per_sm;
+  return per_sm;
 }
 
 template <class S>
-void launch_ray_phases(const RayArgs& a0, cudaStream_t st) {
-  static const int g_march = resident_grid(k_ray_march<S>);
-  static const int g_shade = resident_grid(k_ray_shade<S>);
+int ray_max_per_sm(bool shade) {
+  static const int m = max_per_sm(k_ray_march<S>);
+  static const int h = max_per_sm(k_ray_shade<S>);
+  return shade ? h : m;
+}
+
+int grid_of(int want, int most) { return sm_count() * ((want > 0 && want < most) ? want : most); }
+
+template <class S>
+void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, cudaStream_t st) {
   RayArgs a = a0;
-  k_ray_march<S><<<g_march, kRayThreads, 0, st>>>(a);
+  k_ray_march<S><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
   a.work = a0.work + 4;
-  k_ray_shade<S><<<g_shade, kRayThreads, 0, st>>>(a);
+  k_ray_shade<S><<<grid_of(shape.shade_blocks_per_sm, ray_max_per_sm<S>(true)), kRayThreads, 0, st>>>(a);
 }
 
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate, float* out_depth, float* out_vtx3,
-                    float* out_nrm3, uint8_t* out_img, cudaStream_t st) {
+                    float* out_nrm3, uint8_t* out_img, cudaStream_t st, const LaunchShape& shape) {
   RayArgs a;
   a.bt = bt;
   a.work = const_cast<unsigned*>(bt->work);  // [0..1] march, [4..5] shade
@@ -545,14 +552,25 @@ void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float*
   a.out_img = out_img;
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      launch_ray_phases<StoreF16>(a, st);
+      launch_ray_phases<StoreF16>(a, shape, st);
       break;
     case VS_TSDF_FP32:
-      launch_ray_phases<StoreF32>(a, st);
+      launch_ray_phases<StoreF32>(a, shape, st);
       break;
     default:
-      launch_ray_phases<StoreI16>(a, st);
+      launch_ray_phases<StoreI16>(a, shape, st);
       break;
+  }
+}
+
+int ray_max_blocks_per_sm(int tsdf_type, bool shade) {
+  switch (tsdf_type) {
+    case VS_TSDF_FP16:
+      return ray_max_per_sm<StoreF16>(shade);
+    case VS_TSDF_FP32:
+      return ray_max_per_sm<StoreF32>(shade);
+    default:
+      return ray_max_per_sm<StoreI16>(shade);
   }
 }
 

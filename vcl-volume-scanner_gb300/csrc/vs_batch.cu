@@ -59,6 +59,7 @@ struct vs_batch {
   bool used[kRing] = {false, false};
   cudaGraphExec_t exec[kRing] = {nullptr, nullptr};
   Schedule sched;
+  LaunchShape shape;                           // ray-cast launch shape (autotuned)
   int ring = 0;
   int last = -1;                               // ring slot of the last step
   int kernels = 0;
@@ -88,7 +89,7 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
   launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st);
   mark(3);
   launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
-                 nullptr, nullptr, st);
+                 nullptr, nullptr, st, b->shape);
   mark(4);
   launch_gather_heads(b->d_tab, b->d_heads, st);
   cudaMemcpyAsync(b->h_heads[r], b->d_heads, kMaxSlots * kPoseHeadBytes, cudaMemcpyDeviceToHost, st);
@@ -171,7 +172,7 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
     hr[i] = &ss[i]->h;
     dr[i] = ss[i]->d;
   }
-  fill_batch_table(*b->h_tab[r], hr, dr, n);
+  fill_batch_table(*b->h_tab[r], hr, dr, n, b->shape.ray_lx);
   cudaError_t e = cudaGraphLaunch(b->exec[r], st);
   if (e == cudaSuccess) e = cudaEventRecord(b->done[r], st);
   if (e != cudaSuccess) return cuda_fail_code(e, "batch step launch");
@@ -356,6 +357,96 @@ int vs_batch_get_stage_times(vs_batch* b, float* ms) {
 int vs_batch_kernels_per_step(vs_batch* b) {
   if (!b) return -1;
   return b->exec[0] ? b->kernels : -1;
+}
+
+int vs_batch_get_launch_shape(vs_batch* b, vs_launch_shape* out) {
+  if (!b || !out) return fail_code(VS_ERR_ARG, "null argument");
+  out->ray_tile_log2 = b->shape.ray_lx;
+  out->march_blocks_per_sm = b->shape.march_blocks_per_sm;
+  out->shade_blocks_per_sm = b->shape.shade_blocks_per_sm;
+  return VS_OK;
+}
+
+int vs_batch_set_launch_shape(vs_batch* b, const vs_launch_shape* in) {
+  if (!b || !in) return fail_code(VS_ERR_ARG, "null argument");
+  if (in->ray_tile_log2 < 0 || in->ray_tile_log2 > 5 || in->march_blocks_per_sm < 0 || in->shade_blocks_per_sm < 0 ||
+      in->march_blocks_per_sm > 32 || in->shade_blocks_per_sm > 32)
+    return fail_code(VS_ERR_ARG, "launch shape out of range");
+  int rc = vs_batch_sync(b);
+  if (rc) return rc;
+  b->shape.ray_lx = in->ray_tile_log2;
+  b->shape.march_blocks_per_sm = in->march_blocks_per_sm;
+  b->shape.shade_blocks_per_sm = in->shade_blocks_per_sm;
+  drop_graphs(b);  // recaptured with the new grids at the next step
+  return VS_OK;
+}
+
+// Times the ray-cast stage of these sessions under every candidate launch
+// shape and keeps the fastest.  The ray-cast reads the volume and pose and
+// rewrites the model maps with the values the last step gave them (results
+// do not depend on the shape), so no session changes state.
+int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps, vs_launch_shape* best,
+                      float* best_ms) {
+  if (!b || !sessions) return fail_code(VS_ERR_ARG, "null argument");
+  Schedule k;
+  int rc = check_sessions(b, sessions, n, k);
+  if (rc) return rc;
+  if (reps < 1) reps = 3;
+  rc = vs_batch_sync(b);
+  if (rc) return rc;
+  const SessionDev* hr[kMaxSlots];
+  const SessionDev* dr[kMaxSlots];
+  for (int i = 0; i < n; i++) {
+    hr[i] = &sessions[i]->h;
+    dr[i] = sessions[i]->d;
+  }
+  const int most_m = ray_max_blocks_per_sm(k.tsdf_type, false), most_s = ray_max_blocks_per_sm(k.tsdf_type, true);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaError_t e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  LaunchShape win = b->shape;
+  float win_ms = 1e30f;
+  BatchTable* t = b->h_tab[0];
+  for (int lx = 1; lx <= 5 && e == cudaSuccess; lx++) {
+    fill_batch_table(*t, hr, dr, n, lx);
+    e = cudaMemcpyAsync(b->d_tab, t, sizeof(BatchTable), cudaMemcpyHostToDevice, b->stream);
+    const int mcands[3] = {most_m, (most_m * 3) / 4, most_m / 2};
+    for (int c = 0; c < 3 && e == cudaSuccess; c++) {
+      if (mcands[c] < 1 || (c > 0 && mcands[c] == mcands[c - 1])) continue;
+      LaunchShape sh;
+      sh.ray_lx = lx;
+      sh.march_blocks_per_sm = mcands[c];
+      sh.shade_blocks_per_sm = most_s;
+      // one untimed launch, then reps timed ones
+      for (int r = 0; r <= reps && e == cudaSuccess; r++) {
+        if (r == 1) e = cudaEventRecord(e0, b->stream);
+        launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr,
+                       nullptr, nullptr, nullptr, b->stream, sh);
+        if (e == cudaSuccess) e = cudaGetLastError();
+      }
+      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
+      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+      ms /= (float)reps;
+      if (e == cudaSuccess && ms < win_ms) {
+        win_ms = ms;
+        win = sh;
+      }
+    }
+  }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_autotune");
+  b->shape = win;
+  drop_graphs(b);
+  if (best) {
+    best->ray_tile_log2 = win.ray_lx;
+    best->march_blocks_per_sm = win.march_blocks_per_sm;
+    best->shade_blocks_per_sm = win.shade_blocks_per_sm;
+  }
+  if (best_ms) *best_ms = win_ms;
+  return VS_OK;
 }
 
 }  // extern "C"

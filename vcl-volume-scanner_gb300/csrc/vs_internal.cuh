@@ -105,7 +105,7 @@ struct SessionDev {
 // One session alone is a table of one slot.
 struct BatchTable {
   int n;
-  int pad_;
+  int ray_lx;                          // ray tile of a warp: (1 << ray_lx) x (32 >> ray_lx) rays
   const SessionDev* s[kMaxSlots];
   int bil[kMaxSlots + 1];              // level-0 32x8 tiles (bilateral, activation)
   int pyr[kMaxLevels - 1][kMaxSlots + 1];  // 32x8 tiles of levels 1, 2
@@ -113,7 +113,7 @@ struct BatchTable {
   int ipost[kMaxSlots + 1];            // input-map post-pass 16x16 tiles, all levels
   int scan[kMaxSlots + 1];             // input-map row scans: one per level
   int icp[kMaxLevels][kMaxSlots + 1];  // ICP block ranges per level
-  int ray[kMaxSlots + 1];              // ray-cast 8x4 tiles, all levels
+  int ray[kMaxSlots + 1];              // ray-cast tiles, all levels
   unsigned work[8];                    // work counters ([0..1] ray march, [2..3] ICP, [4..5] ray
                                        // shading); zero between launches
 };
@@ -258,9 +258,20 @@ inline size_t voxel_bytes(int tsdf_type) { return tsdf_type == VS_TSDF_FP32 ? 8 
 // its host copy; grids are fixed (persistent), so a captured graph does not
 // depend on the table's contents.
 // ---------------------------------------------------------------------------
+// Launch shape of the ray-cast kernels.  It changes grid sizes and how rays
+// are grouped into warps, never a ray's computation, so every shape gives
+// the same results (the autotuner picks among them by time).
+struct LaunchShape {
+  int ray_lx = 3;               // ray tile of a warp: (1 << ray_lx) x (32 >> ray_lx), ray_lx in 0..5
+  int march_blocks_per_sm = 0;  // resident 128-thread blocks per SM of the march grid (0: as many as fit)
+  int shade_blocks_per_sm = 0;
+};
+
 int icp_blocks(int npix);
 int sm_count();
-void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n);
+void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n,
+                      int ray_lx = 3);
+int ray_max_blocks_per_sm(int tsdf_type, bool shade);
 void launch_filter(const BatchTable* bt, cudaStream_t st);
 void launch_input_maps(const BatchTable* bt, cudaStream_t st);
 void launch_bilateral_float(const SessionDev& h, const float* in, float* out, cudaStream_t st);
@@ -276,7 +287,8 @@ void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, c
 // one level of a one-slot table into the external outputs with explicit poses
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate_on_tracking, float* out_depth,
-                    float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st);
+                    float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st,
+                    const LaunchShape& shape = LaunchShape());
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st);
 void launch_volume_init(const SessionDev& h, cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);

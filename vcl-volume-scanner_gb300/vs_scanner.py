@@ -106,6 +106,11 @@ class ServerStats(ctypes.Structure):
 
 VS_SESSION_WAITING, VS_SESSION_RESIDENT, VS_SESSION_CLOSED = 0, 1, 2
 
+class LaunchShape(ctypes.Structure):
+    _fields_ = [("ray_tile_log2", ctypes.c_int), ("march_blocks_per_sm", ctypes.c_int),
+                ("shade_blocks_per_sm", ctypes.c_int)]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _F = ctypes.POINTER(ctypes.c_float)
@@ -153,6 +158,9 @@ _SIGS = {
     "vs_batch_set_stage_timing": (_I, [_P, _I]),
     "vs_batch_get_stage_times": (_I, [_P, _P]),
     "vs_batch_kernels_per_step": (_I, [_P]),
+    "vs_batch_get_launch_shape": (_I, [_P, ctypes.POINTER(LaunchShape)]),
+    "vs_batch_set_launch_shape": (_I, [_P, ctypes.POINTER(LaunchShape)]),
+    "vs_batch_autotune": (_I, [_P, _P, _I, _I, ctypes.POINTER(LaunchShape), ctypes.POINTER(ctypes.c_float)]),
     "vs_server_config_default": (None, [ctypes.POINTER(ServerConfig)]),
     "vs_server_create": (_I, [ctypes.POINTER(ServerConfig), ctypes.POINTER(_P)]),
     "vs_server_destroy": (_I, [_P]),
@@ -464,6 +472,23 @@ class Batch:
 
     def kernels_per_step(self):
         return self.lib.vs_batch_kernels_per_step(self.h)
+
+    def launch_shape(self):
+        sh = LaunchShape()
+        _check(self.lib.vs_batch_get_launch_shape(self.h, ctypes.byref(sh)))
+        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm)
+
+    def set_launch_shape(self, ray_tile_log2, march_blocks_per_sm=0, shade_blocks_per_sm=0):
+        sh = LaunchShape(ray_tile_log2, march_blocks_per_sm, shade_blocks_per_sm)
+        _check(self.lib.vs_batch_set_launch_shape(self.h, ctypes.byref(sh)))
+
+    def autotune(self, sessions, reps=3):
+        """picks the fastest ray-cast launch shape for these sessions; returns (shape, ms)"""
+        sh = LaunchShape()
+        ms = ctypes.c_float(0.0)
+        _check(self.lib.vs_batch_autotune(self.h, self._handles(sessions), len(sessions), reps, ctypes.byref(sh),
+                                          ctypes.byref(ms)))
+        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm), ms.value
 
 
 class _Borrowed(Session):
