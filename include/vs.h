@@ -72,6 +72,9 @@ typedef struct {
   int reduce_mode;          /* VS_REDUCE_*                                    */
   int tsdf_type;            /* VS_TSDF_*                                      */
   float depth_scale;        /* uint16 depth units -> metres (0.001)          */
+  int color;                /* 1: keep an RGB volume, integrate and ray-cast
+                               colour (the colour image is registered to the
+                               depth image: same size and intrinsics)       */
 } vs_config;
 
 typedef struct vs_session vs_session;
@@ -128,6 +131,41 @@ int vs_render_maps(vs_session* s, int ww, int hh, const float* T_gc_dev,
                    const float* T_cg_dev, const float* cam_cen, const float* light,
                    int level, float* map_depth_dev, float* map_vertex_dev,
                    float* map_normals_dev, uint8_t* img_normals_dev);
+
+/* ---- colour (sessions created with cfg.color = 1) ------------------------
+ * The colour image is planar uint8 R, G, B, each plane width x height, as the
+ * reference's img_color (plane stride ww*hh), registered to the depth image
+ * (the reference's flag_on_rgb path).  The colour volume holds 8-bit R, G, B
+ * per voxel, initialised to 0. */
+
+/* LGKvVolumeIntegrator::cdtocc_Convert_Depth_to_TSDF_on_Cube_with_Color
+ * (z_yooji_cuda_volume_integrator.cu:265-455): the depth update of
+ * vs_integrate_depth plus, for every updated voxel, the colour sampled
+ * bilinearly at the voxel's projection (d_gii_Get_Interpolated_Intensity,
+ * _yooji_cuda_math.h:305-332) and blended as (w * old + sample) / (w + 1),
+ * truncated to 8 bits.  A sample the reference cannot interpolate (outside
+ * the image, or a texel <= 0) leaves the voxel's colour unchanged (the
+ * reference would blend an uninitialised value). */
+int vs_integrate_depth_color(vs_session* s, const float* map_depth_dev, const uint8_t* img_color_dev, int ww,
+                             int hh, const float* T_gc_dev, const float* T_cg_dev);
+/* rmi_Render_Maps_for_ICP with its img_color output
+ * (z_yooji_cuda_tsdf_renderer.cu:1165-1174): as vs_render_maps plus the
+ * trilinear colour at every hit (d_grvi_Get_RGB_Value_Interpolated,
+ * :232-284), planar uint8, 0 where there is no hit or a neighbour has weight
+ * 0.  img_color_dev: 3 * ww * hh bytes. */
+int vs_render_maps_color(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, int level, float* map_depth_dev,
+                         float* map_vertex_dev, float* map_normals_dev, uint8_t* img_normals_dev,
+                         uint8_t* img_color_dev);
+/* the colour frame the next vs_scan_frame / batch step integrates (planar,
+ * host or device pointer) */
+int vs_set_color_frame(vs_session* s, const uint8_t* img_color, int is_host);
+/* the colour volume in the reference layout: three planes (R, G, B) of
+ * dim[0]*dim[1]*dim[2] bytes, x fastest (cube_color) */
+int vs_get_color_volume(vs_session* s, uint8_t* rgb_host);
+int vs_set_color_volume(vs_session* s, const uint8_t* rgb_host);
+/* the colour image of the last frame's ray-cast at a level, planar */
+int vs_get_color_map(vs_session* s, int level, uint8_t* rgb_host);
 
 /* ---- per-frame hot path (so_Scan_Object) -------------------------------- */
 

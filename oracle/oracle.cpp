@@ -776,6 +776,7 @@ struct Volume {
   std::vector<T> tsdf;
   std::vector<uint16_t> w;
   std::vector<uint8_t> flags;  // 8^3 sub-cube activity of the last frame
+  std::vector<uint8_t> col;    // cube_color: R, G, B planes, x fastest (empty until colour is used)
   int nsc[3];
   void init(const Cfg<T>& c) {
     g = c;
@@ -786,6 +787,10 @@ struct Volume {
     w.assign(n, 0);
     for (int k = 0; k < 3; k++) nsc[k] = (g.dim[k] + 7) / 8;
     flags.assign((size_t)nsc[0] * nsc[1] * nsc[2], 0);
+    col.clear();
+  }
+  void enable_color() {
+    if (col.empty()) col.assign((size_t)3 * g.dim[0] * g.dim[1] * g.dim[2], 0);
   }
 };
 
@@ -860,6 +865,91 @@ void update_tsdf(Volume<T>& V, const float* depth, const T* T_gc, const T* T_cg)
               V.w[idx] = (uint16_t)newW;
             }
       }
+}
+
+// d_gii_Get_Interpolated_Intensity (_yooji_cuda_math.h:305-332) on one 8-bit
+// plane: bilinear, a used texel <= 0 fails; NaN coordinates fail (the
+// reference's comparisons let them through to an undefined conversion).
+template <class T>
+bool interp_intensity(T xf, T yf, int w, int h, const uint8_t* map, T& out) {
+  if (!(xf >= T(0) && xf <= (T)(w - 1) && yf >= T(0) && yf <= (T)(h - 1))) return false;
+  int x = (int)xf, y = (int)yf;
+  T rx = xf - (T)x, ry = yf - (T)y;
+  T d2 = 0, d3 = 0, d4 = 0;
+  T d1 = (T)map[(size_t)y * w + x];
+  if (d1 <= T(0)) return false;
+  if (rx > T(0)) {
+    d2 = (T)map[(size_t)y * w + x + 1];
+    if (d2 <= T(0)) return false;
+  }
+  if (ry > T(0)) {
+    d3 = (T)map[(size_t)(y + 1) * w + x];
+    if (d3 <= T(0)) return false;
+  }
+  if (rx > T(0) && ry > T(0)) {
+    d4 = (T)map[(size_t)(y + 1) * w + x + 1];
+    if (d4 <= T(0)) return false;
+  }
+  out = (T(1) - ry) * ((T(1) - rx) * d1 + rx * d2) + ry * ((T(1) - rx) * d3 + rx * d4);
+  return true;
+}
+
+// g_ctvc_Compute_TSDF_of_Voxels_with_Color, depth and colour
+// (z_yooji_cuda_volume_integrator.cu:265-455), registered colour
+// (flag_on_rgb: the colour is sampled at the voxel's projection into the
+// depth camera).  The colour planes have the depth image's size, as the
+// reference indexes them (&img_color[k*ww*hh]).  A channel that cannot be
+// interpolated leaves the voxel's colour unchanged (the reference would blend
+// an uninitialised value).
+template <class T>
+void update_tsdf_color(Volume<T>& V, const float* depth, const uint8_t* rgb, const T* T_gc, const T* T_cg) {
+  const Cfg<T>& g = V.g;
+  const int w = g.W[0], h = g.H[0];
+  const T* K = g.K[0];
+  const int X = g.dim[0], Y = g.dim[1];
+  const size_t n3 = (size_t)X * Y * g.dim[2], n2 = (size_t)w * h;
+  V.enable_color();
+  const int nsc = V.nsc[0] * V.nsc[1] * V.nsc[2];
+#pragma omp parallel for schedule(dynamic, 16)
+  for (int sc = 0; sc < nsc; sc++) {
+    const int xs = sc % V.nsc[0], ys = (sc / V.nsc[0]) % V.nsc[1], zs = sc / (V.nsc[0] * V.nsc[1]);
+    if (!V.flags[sc]) continue;
+    for (int lz = 0; lz < 8; lz++)
+      for (int ly = 0; ly < 8; ly++)
+        for (int lx = 0; lx < 8; lx++) {
+          int xc = xs * 8 + lx, yc = ys * 8 + ly, zc = zs * 8 + lz;
+          V3<T> pg = pos_in_world(v3<T>((T)xc, (T)yc, (T)zc), g.origin, g.vox_inv);
+          V3<T> pc = transform(pg, T_gc);
+          T u, v;
+          project(pc, K, u, v);
+          int x = float2int_rn(u), y = float2int_rn(v);
+          if (x < 0 || x > w - 1 || y < 0 || y > h - 1) continue;
+          T dm = (T)depth[(size_t)y * w + x];
+          if (!(dm > T(0))) continue;
+          V3<T> r = back_project((T)x, (T)y, K, T(1));
+          T lam = T(1) / tsqrt(r.x * r.x + r.y * r.y + T(1));
+          V3<T> dc = v3(pg.x - T_cg[3], pg.y - T_cg[7], pg.z - T_cg[11]);
+          T nrm = tsqrt(dc.x * dc.x + dc.y * dc.y + dc.z * dc.z);
+          T sdf = dm - lam * nrm;
+          if (sdf < -g.mu) continue;
+          T ts = std::fmin(T(1), sdf / g.mu);
+          size_t idx = ((size_t)zc * Y + yc) * X + xc;
+          T oldW = (T)V.w[idx];
+          T newW = oldW + T(1);
+          T inewW = T(1) / newW;
+          if (oldW >= g.max_w) continue;
+          V.tsdf[idx] = store_tsdf<T>((oldW * V.tsdf[idx] + ts) * inewW, g.tsdf_store);
+          V.w[idx] = (uint16_t)newW;
+          T smp[3];
+          bool ok = true;
+          for (int k = 0; k < 3; k++) ok = ok && interp_intensity(u, v, w, h, rgb + k * n2, smp[k]);
+          if (!ok) continue;
+          for (int k = 0; k < 3; k++) {
+            uint8_t& c = V.col[idx + k * n3];
+            c = (uint8_t)(std::fmax(T(0), std::fmin(T(255.0f), (oldW * (T)c + smp[k]) * inewW)));
+          }
+        }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -1047,9 +1137,45 @@ bool cast_ray(const Volume<T>& V, int lev, T px, T py, const T* T_cg, V3<T> cam,
   return false;
 }
 
+// d_grvi_Get_RGB_Value_Interpolated (z_yooji_cuda_tsdf_renderer.cu:232-284)
+// with d_grvu (:194-229) for the eight neighbours (in range, weight > 0), and
+// InfiniTAM's Vector3f::toUChar: round half away from zero, clamp 0..255.
+template <class T>
+void trilinear_color(const Volume<T>& V, V3<T> pg, uint8_t out[3]) {
+  out[0] = out[1] = out[2] = 0;
+  if (V.col.empty()) return;
+  const Cfg<T>& g = V.g;
+  V3<T> pv;
+  pos_in_voxel(pg, g.origin, g.dim, g.vox_inv, pv);
+  if (std::isnan(pv.x) || std::isnan(pv.y) || std::isnan(pv.z)) return;
+  int o[3];
+  V3<T> r;
+  to_int_floor(pv, o, r);
+  const size_t n3 = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
+  size_t idx[8];
+  for (int i = 0; i < 8; i++) {
+    int x = o[0] + (i & 1), y = o[1] + ((i >> 1) & 1), z = o[2] + (i >> 2);
+    if (x < 0 || x >= g.dim[0] || y < 0 || y >= g.dim[1] || z < 0 || z >= g.dim[2]) return;
+    idx[i] = ((size_t)z * g.dim[1] + y) * g.dim[0] + x;
+    if (V.w[idx[i]] == 0) return;
+  }
+  for (int k = 0; k < 3; k++) {
+    T f[4], b[4];
+    for (int i = 0; i < 4; i++) {
+      f[i] = (T)V.col[idx[i] + k * n3];
+      b[i] = (T)V.col[idx[4 + i] + k * n3];
+    }
+    T inf = (T(1) - r.y) * ((T(1) - r.x) * f[0] + r.x * f[1]) + r.y * ((T(1) - r.x) * f[2] + r.x * f[3]);
+    T inb = (T(1) - r.y) * ((T(1) - r.x) * b[0] + r.x * b[1]) + r.y * ((T(1) - r.x) * b[2] + r.x * b[3]);
+    T val = (T(1) - r.z) * inf + r.z * inb;
+    T rounded = (val < T(0)) ? (val - T(0.5f)) : (val + T(0.5f));
+    out[k] = (uint8_t)std::fmax(T(0), std::fmin(T(255.0f), rounded));
+  }
+}
+
 template <class T>
 void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> cam, V3<T> light,
-             T* depth, T* vtx, T* nrm, uint8_t* img) {
+             T* depth, T* vtx, T* nrm, uint8_t* img, uint8_t* rgb = nullptr) {
   const Cfg<T>& g = V.g;
   const int w = g.W[lev], h = g.H[lev];
   V3<T> cc = v3(g.center[0], g.center[1], g.center[2]);
@@ -1077,11 +1203,18 @@ void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> ca
         T s = (T(0.8f) * ang + T(0.2f)) * T(255.0f);
         s = std::fmax(T(0), std::fmin(T(255.0f), s));
         img[t] = (uint8_t)s;
+        if (rgb) {
+          uint8_t c[3];
+          trilinear_color(V, pg, c);
+          for (int k = 0; k < 3; k++) rgb[t + k * (size_t)w * h] = c[k];
+        }
       } else {
         depth[t] = 0;
         vtx[3 * t] = vtx[3 * t + 1] = vtx[3 * t + 2] = T(-100);
         nrm[3 * t] = nrm[3 * t + 1] = nrm[3 * t + 2] = T(-100);
         img[t] = 0;
+        if (rgb)
+          for (int k = 0; k < 3; k++) rgb[t + k * (size_t)w * h] = 0;
       }
     }
 }
@@ -1275,6 +1408,24 @@ void or_volume_flags(const or_volume* v, uint8_t* flags) {
 void or_integrate(or_volume* v, const float* depth, const float* T_gc, const float* T_cg) {
   find_visible_subcubes(v->v, depth, T_cg);
   update_tsdf(v->v, depth, T_gc, T_cg);
+}
+void or_integrate_color(or_volume* v, const float* depth, const uint8_t* rgb, const float* T_gc,
+                        const float* T_cg) {
+  find_visible_subcubes(v->v, depth, T_cg);
+  update_tsdf_color(v->v, depth, rgb, T_gc, T_cg);
+}
+void or_volume_get_color(or_volume* v, uint8_t* rgb) {
+  v->v.enable_color();
+  std::memcpy(rgb, v->v.col.data(), v->v.col.size());
+}
+void or_volume_set_color(or_volume* v, const uint8_t* rgb) {
+  v->v.enable_color();
+  std::memcpy(v->v.col.data(), rgb, v->v.col.size());
+}
+void or_raycast_color(const or_volume* v, int level, const float* T_gc, const float* T_cg, const float* cam_cen,
+                      const float* light, float* depth, float* vtx3, float* nrm3, uint8_t* img, uint8_t* rgb) {
+  raycast<float>(v->v, level, T_gc, T_cg, v3(cam_cen[0], cam_cen[1], cam_cen[2]),
+                 v3(light[0], light[1], light[2]), depth, vtx3, nrm3, img, rgb);
 }
 void or_raycast(const or_volume* v, int level, const float* T_gc, const float* T_cg,
                 const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,

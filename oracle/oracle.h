@@ -100,6 +100,16 @@ void or_integrate(or_volume* v, const float* depth, const float* T_gc,
                   const float* T_cg);
 /* reference raycast of one level.  cam_cen / light: float3.
  * outputs: depth W*H, vertex/normal AoS float3, shaded image uint8. */
+/* colour: g_ctvc with colour (registered colour image, planar R, G, B of the
+ * depth image's size), the colour volume (three x-fastest planes), and the
+ * ray-cast with the colour image (planar) */
+void or_integrate_color(or_volume* v, const float* depth, const uint8_t* rgb, const float* T_gc,
+                        const float* T_cg);
+void or_volume_get_color(or_volume* v, uint8_t* rgb);
+void or_volume_set_color(or_volume* v, const uint8_t* rgb);
+void or_raycast_color(const or_volume* v, int level, const float* T_gc, const float* T_cg,
+                      const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,
+                      uint8_t* img, uint8_t* rgb);
 void or_raycast(const or_volume* v, int level, const float* T_gc,
                 const float* T_cg, const float* cam_cen, const float* light,
                 float* depth, float* vtx3, float* nrm3, uint8_t* img);

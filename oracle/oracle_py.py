@@ -73,6 +73,10 @@ def load():
             "or_volume_flags": (None, [P, P]),
             "or_integrate": (None, [P, P, P, P]),
             "or_raycast": (None, [P, I, P, P, P, P, P, P, P, P]),
+            "or_integrate_color": (None, [P, P, P, P, P]),
+            "or_volume_get_color": (None, [P, P]),
+            "or_volume_set_color": (None, [P, P]),
+            "or_raycast_color": (None, [P, I, P, P, P, P, P, P, P, P, P]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
             "or_session_destroy": (None, [P]),
@@ -289,6 +293,39 @@ class Volume:
         a = np.ascontiguousarray(T_gc, np.float32).reshape(16)
         b = np.ascontiguousarray(T_cg, np.float32).reshape(16)
         self.lib.or_integrate(self.h, _p(d), _p(a), _p(b))
+
+    def integrate_color(self, depth_m, rgb, T_gc, T_cg):
+        """rgb: planar uint8 (3, h, w) of the depth image's size"""
+        d = np.ascontiguousarray(depth_m, np.float32)
+        c = np.ascontiguousarray(rgb, np.uint8)
+        a = np.ascontiguousarray(T_gc, np.float32).reshape(16)
+        b = np.ascontiguousarray(T_cg, np.float32).reshape(16)
+        self.lib.or_integrate_color(self.h, _p(d), _p(c), _p(a), _p(b))
+
+    def get_color(self):
+        out = np.empty(3 * self.n, np.uint8)
+        self.lib.or_volume_get_color(self.h, _p(out))
+        return out.reshape(3, self.n)
+
+    def set_color(self, rgb):
+        c = np.ascontiguousarray(rgb, np.uint8)
+        assert c.size == 3 * self.n
+        self.lib.or_volume_set_color(self.h, _p(c))
+
+    def raycast_color(self, level, T_gc, T_cg, cam, light=(0.0, 0.0, -1.0)):
+        w, h = level_sizes(self.cfg)[level]
+        a = np.ascontiguousarray(T_gc, np.float32).reshape(16)
+        b = np.ascontiguousarray(T_cg, np.float32).reshape(16)
+        c = np.ascontiguousarray(cam, np.float32)
+        l = np.ascontiguousarray(light, np.float32)
+        dep = np.empty((h, w), np.float32)
+        v = np.empty((h, w, 3), np.float32)
+        n = np.empty((h, w, 3), np.float32)
+        img = np.empty((h, w), np.uint8)
+        rgb = np.empty((3, h, w), np.uint8)
+        self.lib.or_raycast_color(self.h, level, _p(a), _p(b), _p(c), _p(l), _p(dep), _p(v), _p(n), _p(img),
+                                  _p(rgb))
+        return dep, v, n, img, rgb
 
     def raycast(self, level, T_gc, T_cg, cam, light=(0.0, 0.0, -1.0)):
         w, h = level_sizes(self.cfg)[level]

@@ -93,6 +93,14 @@ __global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __
     const float g[5] = {s->gauss[0], s->gauss[1], s->gauss[2], s->gauss[1], s->gauss[0]};
     bilateral_tile<true>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
                          (t / tw) * BY, g);
+    if (s->rgb_packed) {
+      // the colour frame as one word per pixel, for the integration's gathers
+      const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * BY + threadIdx.y;
+      if (x < W && y < H) {
+        const size_t i = (size_t)y * W + x, plane = (size_t)W * H;
+        s->rgb_packed[i] = pack_rgb(s->rgb_in[i], s->rgb_in[plane + i], s->rgb_in[2 * plane + i]);
+      }
+    }
     __syncthreads();  // the next tile overwrites the shared tiles
   }
 }

@@ -132,6 +132,8 @@ struct IntParams {
   uint32_t* occ1;
   uint32_t* occ2;
   void* vol;
+  uint32_t* col;            // colour bricks (NULL: no colour)
+  const uint32_t* rgb;      // packed colour frame
   float T[12];
   float C[3];
   float K[4];
@@ -157,6 +159,8 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.nc2[0] = s->nc2[0];
   q.nc2[1] = s->nc2[1];
   q.vol = s->vol;
+  q.col = s->col;
+  q.rgb = s->rgb_packed;
   const float* Tgc = Tgc_ext ? Tgc_ext : s->pose->Tgc;
   const float* Tcg = Tcg_ext ? Tcg_ext : s->pose->Tcg;
 #pragma unroll
@@ -176,14 +180,98 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.d1 = s->dim[1];
 }
 
+// The colour part of g_ctvc (z_yooji_cuda_volume_integrator.cu:404-455, the
+// registered-colour path): for every voxel of the round whose depth was just
+// updated, the colour at its projection, interpolated as
+// d_gii_Get_Interpolated_Intensity (_yooji_cuda_math.h:305-332) per channel,
+// is blended as (w * old + sample) / (w + 1) and truncated to 8 bits.  When a
+// channel cannot be interpolated (outside the image, or a used texel <= 0) the
+// voxel keeps its colour (the reference would blend an uninitialised value).
+// The four taps and the old colour of four voxels are read in one round.
+__device__ inline bool interp_channel(uint32_t a, uint32_t b, uint32_t c, uint32_t d, int k, float rx, float ry,
+                                      float& out) {
+  const float d1 = (float)rgb_channel(a, k);
+  if (d1 <= 0.0f) return false;
+  float d2 = 0.0f, d3 = 0.0f, d4 = 0.0f;
+  if (rx > 0.0f) {
+    d2 = (float)rgb_channel(b, k);
+    if (d2 <= 0.0f) return false;
+  }
+  if (ry > 0.0f) {
+    d3 = (float)rgb_channel(c, k);
+    if (d3 <= 0.0f) return false;
+  }
+  if (rx > 0.0f && ry > 0.0f) {
+    d4 = (float)rgb_channel(d, k);
+    if (d4 <= 0.0f) return false;
+  }
+  out = (1.0f - ry) * ((1.0f - rx) * d1 + rx * d2) + ry * ((1.0f - rx) * d3 + rx * d4);
+  return true;
+}
+
+template <class S, int kPerVec, class IP, class WV>
+__device__ void color_round(const IP& q, unsigned upd, int v0, int lane, int bx, int by, int bz, uint32_t b,
+                            const WV& wv, const float* __restrict__ lx, const float* __restrict__ ly,
+                            const float* __restrict__ lz) {
+  constexpr int kG = 4;
+#pragma unroll
+  for (int g = 0; g < 8; g += kG) {
+    uint32_t t00[kG], t01[kG], t10[kG], t11[kG], oc[kG];
+    float rxs[kG], rys[kG];
+    bool ok[kG];
+#pragma unroll
+    for (int j = 0; j < kG; j++) {
+      ok[j] = false;
+      if (!((upd >> (g + j)) & 1u)) continue;
+      const int v = v0 + g + j, k = v / kPerVec, e = v % kPerVec;
+      const int li = (k * 32 + lane) * kPerVec + e;
+      const int xc = bx * 8 + (li & 7), yc = by * 8 + ((li >> 3) & 7), zc = bz * 8 + (li >> 6);
+      const F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
+      float u, vv;
+      project(transform(pg, q.T), q.K, u, vv);
+      if (!(u >= 0.0f && u <= (float)(q.W - 1) && vv >= 0.0f && vv <= (float)(q.H - 1))) continue;
+      const int x = (int)u, y = (int)vv;
+      rxs[j] = u - (float)x;
+      rys[j] = vv - (float)y;
+      const int xb = rxs[j] > 0.0f ? x + 1 : x, yb = rys[j] > 0.0f ? y + 1 : y;
+      t00[j] = __ldg(q.rgb + y * q.W + x);
+      t01[j] = __ldg(q.rgb + y * q.W + xb);
+      t10[j] = __ldg(q.rgb + yb * q.W + x);
+      t11[j] = __ldg(q.rgb + yb * q.W + xb);
+      oc[j] = q.col[(size_t)b * kBrickVox + li];
+      ok[j] = true;
+    }
+#pragma unroll
+    for (int j = 0; j < kG; j++) {
+      if (!ok[j]) continue;
+      const int v = v0 + g + j, k = v / kPerVec, e = v % kPerVec;
+      const int li = (k * 32 + lane) * kPerVec + e;
+      float tn;
+      uint32_t wn;
+      S::decode(wv[k][e], tn, wn);  // the updated word: weight w + 1
+      const float oldW = (float)(wn - 1u), inewW = __ldg(g_inv_weight + wn);
+      float smp[3];
+      bool good = true;
+#pragma unroll
+      for (int c = 0; c < 3; c++) good &= interp_channel(t00[j], t01[j], t10[j], t11[j], c, rxs[j], rys[j], smp[c]);
+      if (!good) continue;
+      uint32_t ch[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++)
+        ch[c] = (uint32_t)(uint8_t)(fmaxf(0.0f, fminf(255.0f, (oldW * (float)rgb_channel(oc[j], c) + smp[c]) * inewW)));
+      q.col[(size_t)b * kBrickVox + li] = pack_rgb(ch[0], ch[1], ch[2]);
+    }
+  }
+}
+
 #ifndef VS_INT_MIN_BLOCKS
 #define VS_INT_MIN_BLOCKS 2  // resident 256-thread blocks per SM the register allocation must allow
 #endif
 
-template <class S>
+template <class S, bool COLOR>
 __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
     k_integrate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
-                const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext) {
+                const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext, int color) {
   __shared__ uint32_t pre[kMaxSlots + 1];  // prefix of the slots' active-brick counts
   const int n = bt->n;
   if (threadIdx.x < 32) {
@@ -227,6 +315,7 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
     if (lo != cur) {
       cur = lo;
       load_params(q, bt->s[lo], depth_ext, Tgc_ext, Tcg_ext);
+      if (!color) q.col = nullptr;
     }
     const uint32_t b = q.list[i - pre[lo]];
     int nupd = 0;
@@ -253,6 +342,7 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
     for (int r = 0; r < kLaneVox / kRound; r++) {
       int pix[kRound];
       float dm[kRound], lam[kRound];
+      unsigned upd = 0u;  // voxels of this round whose depth was updated
 #pragma unroll
       for (int j = 0; j < kRound; j++) {
         const int v = r * kRound + j, k = v / kPerVec, e = v % kPerVec;
@@ -307,8 +397,10 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
         const float tnew = (oldW * told + ts) * inewW;
         wv[k][e] = S::encode(tnew, (uint32_t)newW);
         changed[k] = true;
+        upd |= 1u << j;
         nupd++;
       }
+      if (COLOR && q.col && upd) color_round<S, kPerVec>(q, upd, r * kRound, lane, bx, by, bz, b, wv, lx, ly, lz);
     }
 #pragma unroll
     for (int k = 0; k < kLaneVec; k++)
@@ -402,7 +494,55 @@ __global__ void k_occupancy(const SessionDev* __restrict__ s) {
   }
 }
 
+__global__ void k_pack_color(const uint8_t* __restrict__ rgb, uint32_t* __restrict__ out, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = pack_rgb(rgb[i], rgb[n + i], rgb[2 * n + i]);
+}
+
+// bricked colour words <-> three planes of x-fastest bytes (cube_color)
+__global__ void k_color_volume(uint32_t* col, int X, int Y, int Z, int nb0, int nb1, uint8_t* planes, int do_export) {
+  const size_t n = (size_t)X * Y * Z;
+  int nb[3] = {nb0, nb1, 0};
+  for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    const int x = (int)(i % X), y = (int)((i / X) % Y), z = (int)(i / ((size_t)X * Y));
+    const size_t w = brick_word_index(x, y, z, nb);
+    if (do_export) {
+      const uint32_t c = col[w];
+      planes[i] = (uint8_t)rgb_channel(c, 0);
+      planes[n + i] = (uint8_t)rgb_channel(c, 1);
+      planes[2 * n + i] = (uint8_t)rgb_channel(c, 2);
+    } else {
+      col[w] = pack_rgb(planes[i], planes[n + i], planes[2 * n + i]);
+    }
+  }
+}
+
+__global__ void k_color_map_export(const uint32_t* __restrict__ m, int n, uint8_t* __restrict__ planes) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    const uint32_t c = m[i];
+    planes[i] = (uint8_t)rgb_channel(c, 0);
+    planes[n + i] = (uint8_t)rgb_channel(c, 1);
+    planes[2 * n + i] = (uint8_t)rgb_channel(c, 2);
+  }
+}
+
 }  // namespace
+
+void launch_pack_color(const SessionDev& h, const uint8_t* rgb, cudaStream_t st) {
+  const int n = h.lv[0].W * h.lv[0].H;
+  k_pack_color<<<(n + 255) / 256, 256, 0, st>>>(rgb ? rgb : h.rgb_in, h.rgb_packed, n);
+}
+
+void launch_color_volume(const SessionDev& h, bool do_export, uint8_t* planes, cudaStream_t st) {
+  k_color_volume<<<sm_count() * 8, 256, 0, st>>>(h.col, h.dim[0], h.dim[1], h.dim[2], h.nb[0], h.nb[1], planes,
+                                                 do_export ? 1 : 0);
+}
+
+void launch_color_map_export(const SessionDev& h, int level, uint8_t* planes, cudaStream_t st) {
+  const int n = h.lv[level].W * h.lv[level].H;
+  k_color_map_export<<<(n + 255) / 256, 256, 0, st>>>(h.m_rgb[level], n, planes);
+}
 
 int sm_count() {
   static int n = 0;
@@ -415,17 +555,27 @@ int sm_count() {
   return n;
 }
 
-template <class S>
+template <class S, bool COLOR>
 int resident_blocks() {
-  // one query per storage type (the answer depends only on the compiled kernel)
+  // one query per kernel variant (the answer depends only on the compiled kernel)
   static int per_sm = -1;
   if (per_sm < 0) {
     int v = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_integrate<S>, kIntThreads, 0) != cudaSuccess || v < 1)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_integrate<S, COLOR>, kIntThreads, 0) != cudaSuccess ||
+        v < 1)
       v = 1;
     per_sm = v;
   }
   return sm_count() * per_sm;
+}
+
+template <class S>
+void launch_update(const BatchTable* bt, const float* depth, const float* Tgc, const float* Tcg, bool color,
+                   cudaStream_t st) {
+  if (color)
+    k_integrate<S, true><<<resident_blocks<S, true>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 1);
+  else
+    k_integrate<S, false><<<resident_blocks<S, false>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 0);
 }
 
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) {
@@ -435,19 +585,20 @@ void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) 
 }
 
 void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc, const float* Tcg,
-                      bool gate, cudaStream_t st) {
+                      bool gate, cudaStream_t st, bool color) {
+  const int c = color ? 1 : 0;
   k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt);
   k_activate<<<sm_count() * 8, dim3(32, 8), 0, st>>>(bt, depth, Tcg, gate ? 1 : 0);
   // persistent grid: every block resident at once
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      k_integrate<StoreF16><<<resident_blocks<StoreF16>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      launch_update<StoreF16>(bt, depth, Tgc, Tcg, c != 0, st);
       break;
     case VS_TSDF_FP32:
-      k_integrate<StoreF32><<<resident_blocks<StoreF32>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      launch_update<StoreF32>(bt, depth, Tgc, Tcg, c != 0, st);
       break;
     default:
-      k_integrate<StoreI16><<<resident_blocks<StoreI16>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg);
+      launch_update<StoreI16>(bt, depth, Tgc, Tcg, c != 0, st);
       break;
   }
 }

@@ -42,6 +42,7 @@ struct RayArgs {
   float* out_vtx3;
   float* out_nrm3;
   uint8_t* out_img;
+  uint8_t* out_rgb;     // planar colour image (NULL: none)
 };
 
 // Volume reads.  A brick whose occupancy bit is clear has weight 0 in every
@@ -437,9 +438,52 @@ __global__ void __launch_bounds__(kRayThreads, VS_RAY_MIN_BLOCKS) k_ray_march(Ra
   });
 }
 
-// phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
-// normal, shading, into the model maps or the external outputs
+// d_grvi_Get_RGB_Value_Interpolated (z_yooji_cuda_tsdf_renderer.cu:232-284):
+// trilinear colour of the eight voxels around the hit, every one in range with
+// weight > 0 (d_grvu, :194-229), rounded to 8 bits as InfiniTAM's toUChar
+// (round half away from zero, clamp to 0..255); 0 when a neighbour fails.
+// The 16 reads (weights and colours) are issued before any test.
 template <class S>
+__device__ uint32_t trilinear_color(const Vol<S>& V, const SessionDev& s, F3 pg) {
+  F3 v;
+  pos_in_voxel(pg, s, v);
+  if (isnan(v.x) || isnan(v.y) || isnan(v.z)) return 0u;
+  const float fx = floorf(v.x), fy = floorf(v.y), fz = floorf(v.z);
+  const int ox = (int)fx, oy = (int)fy, oz = (int)fz;
+  const float rx = v.x - fx, ry = v.y - fy, rz = v.z - fz;
+  float tdummy;
+  bool ok = true;
+  uint32_t c[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const int x = ox + (i & 1), y = oy + ((i >> 1) & 1), z = oz + (i >> 2);
+    const bool in = x >= 0 && x < V.dim[0] && y >= 0 && y < V.dim[1] && z >= 0 && z < V.dim[2];
+    const size_t w = in ? brick_word_index(x, y, z, V.nb) : 0;
+    ok &= V.at_any(x, y, z, tdummy);
+    c[i] = __ldg(s.col + w);
+  }
+  if (!ok) return 0u;
+  uint32_t out[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    float f[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+      f[i] = (float)rgb_channel(c[i], k);
+      b[i] = (float)rgb_channel(c[4 + i], k);
+    }
+    const float inf = (1.0f - ry) * ((1.0f - rx) * f[0] + rx * f[1]) + ry * ((1.0f - rx) * f[2] + rx * f[3]);
+    const float inb = (1.0f - ry) * ((1.0f - rx) * b[0] + rx * b[1]) + ry * ((1.0f - rx) * b[2] + rx * b[3]);
+    const float val = (1.0f - rz) * inf + rz * inb;
+    const float rounded = (val < 0.0f) ? (val - 0.5f) : (val + 0.5f);
+    out[k] = (uint32_t)(uint8_t)fmaxf(0.0f, fminf(255.0f, rounded));
+  }
+  return pack_rgb(out[0], out[1], out[2]);
+}
+
+// phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
+// normal, shading, colour, into the model maps or the external outputs
+template <class S, bool COLOR>
 __global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(RayArgs a) {
   for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
     const Vol<S> V = volume_of<S>(s);
@@ -451,8 +495,10 @@ __global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(
     bool valid = h.w != 0.0f;
     if (valid) valid = surface_normal(V, s, pg, sn);
     float dep = 0.0f, img = 0.0f;
+    uint32_t rgb = 0u;
     F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
     if (valid) {
+      if (COLOR && s.col) rgb = trilinear_color(V, s, pg);
       const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
       float Tgc[12];
 #pragma unroll
@@ -472,12 +518,19 @@ __global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(
       a.out_nrm3[3 * idx + 1] = sc.y;
       a.out_nrm3[3 * idx + 2] = sc.z;
       if (a.out_img) a.out_img[idx] = (uint8_t)img;
+      if (COLOR && a.out_rgb) {
+        const size_t plane = (size_t)s.lv[l].W * s.lv[l].H;
+        a.out_rgb[idx] = (uint8_t)rgb_channel(rgb, 0);
+        a.out_rgb[plane + idx] = (uint8_t)rgb_channel(rgb, 1);
+        a.out_rgb[2 * plane + idx] = (uint8_t)rgb_channel(rgb, 2);
+      }
     } else {
       const float vw = valid ? 1.0f : 0.0f;
       s.m_depth[l][idx] = dep;
       s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
       s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
       s.m_img[l][idx] = (uint8_t)img;
+      if (COLOR && s.col) s.m_rgb[l][idx] = rgb;
     }
   });
 }
@@ -518,23 +571,28 @@ int max_per_sm(K kernel) {
 template <class S>
 int ray_max_per_sm(bool shade) {
   static const int m = max_per_sm(k_ray_march<S>);
-  static const int h = max_per_sm(k_ray_shade<S>);
+  static const int h = max_per_sm(k_ray_shade<S, false>);
   return shade ? h : m;
 }
 
 int grid_of(int want, int most) { return sm_count() * ((want > 0 && want < most) ? want : most); }
 
 template <class S>
-void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, cudaStream_t st) {
+void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, bool color, cudaStream_t st) {
   RayArgs a = a0;
   k_ray_march<S><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
   a.work = a0.work + 4;
-  k_ray_shade<S><<<grid_of(shape.shade_blocks_per_sm, ray_max_per_sm<S>(true)), kRayThreads, 0, st>>>(a);
+  static const int most_color = max_per_sm(k_ray_shade<S, true>);
+  if (color)
+    k_ray_shade<S, true><<<grid_of(shape.shade_blocks_per_sm, most_color), kRayThreads, 0, st>>>(a);
+  else
+    k_ray_shade<S, false><<<grid_of(shape.shade_blocks_per_sm, ray_max_per_sm<S>(true)), kRayThreads, 0, st>>>(a);
 }
 
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate, float* out_depth, float* out_vtx3,
-                    float* out_nrm3, uint8_t* out_img, cudaStream_t st, const LaunchShape& shape) {
+                    float* out_nrm3, uint8_t* out_img, cudaStream_t st, const LaunchShape& shape, uint8_t* out_rgb,
+                    bool color) {
   RayArgs a;
   a.bt = bt;
   a.work = const_cast<unsigned*>(bt->work);  // [0..1] march, [4..5] shade
@@ -550,15 +608,16 @@ void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float*
   a.out_vtx3 = out_vtx3;
   a.out_nrm3 = out_nrm3;
   a.out_img = out_img;
+  a.out_rgb = out_rgb;
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      launch_ray_phases<StoreF16>(a, shape, st);
+      launch_ray_phases<StoreF16>(a, shape, color, st);
       break;
     case VS_TSDF_FP32:
-      launch_ray_phases<StoreF32>(a, shape, st);
+      launch_ray_phases<StoreF32>(a, shape, color, st);
       break;
     default:
-      launch_ray_phases<StoreI16>(a, shape, st);
+      launch_ray_phases<StoreI16>(a, shape, color, st);
       break;
   }
 }

@@ -206,7 +206,26 @@ void vs_synth_default(vs_synth_config* c, int width, int height) {
   c->threads = 0;
 }
 
+static int generate(const vs_synth_config* c, uint16_t* depth, uint8_t* rgb, double* T_gc, double* centre_cam0);
+
 int vs_synth_generate(const vs_synth_config* c, uint16_t* depth, double* T_gc, double* centre_cam0) {
+  return generate(c, depth, nullptr, T_gc, centre_cam0);
+}
+
+int vs_synth_generate_rgb(const vs_synth_config* c, uint16_t* depth, uint8_t* rgb, double* T_gc,
+                          double* centre_cam0) {
+  if (!rgb) return -1;
+  return generate(c, depth, rgb, T_gc, centre_cam0);
+}
+
+// colour of a surface point (scene frame): a smooth procedural texture, every
+// channel in 30..230 so a hit never reads as "no colour"
+static void surface_rgb(const double* P, uint8_t out[3]) {
+  const double f[3] = {9.0 * P[0], 7.0 * P[2] + 1.0, 11.0 * P[1] + 2.0};
+  for (int k = 0; k < 3; k++) out[k] = (uint8_t)(30.0 + 200.0 * (0.5 + 0.5 * std::sin(f[k])) + 0.5);
+}
+
+static int generate(const vs_synth_config* c, uint16_t* depth, uint8_t* rgb, double* T_gc, double* centre_cam0) {
   if (!c || c->width <= 0 || c->height <= 0 || c->n_frames <= 0) return -1;
   Scene s = make_scene(c->seed);
   const int W = c->width, H = c->height, N = c->n_frames;
@@ -240,6 +259,7 @@ int vs_synth_generate(const vs_synth_config* c, uint16_t* depth, double* T_gc, d
       std::memcpy(T_gc + 16 * (size_t)k, O, sizeof(O));
     }
     uint16_t* out = depth + (size_t)k * W * H;
+    uint8_t* col = rgb ? rgb + (size_t)k * 3 * W * H : nullptr;
     auto rows = [&](int r0, int r1) {
       for (int v = r0; v < r1; v++)
         for (int u = 0; u < W; u++) {
@@ -249,6 +269,14 @@ int vs_synth_generate(const vs_synth_config* c, uint16_t* depth, double* T_gc, d
           double t = hit(s, pos, d);
           double z = (t < 1e29) ? t : 0.0;
           uint64_t pk = (uint64_t)v * W + u;
+          if (col) {
+            uint8_t cc[3] = {0, 0, 0};
+            if (t < 1e29) {
+              const double P[3] = {pos[0] + t * d[0], pos[1] + t * d[1], pos[2] + t * d[2]};
+              surface_rgb(P, cc);
+            }
+            for (int ch = 0; ch < 3; ch++) col[(size_t)ch * W * H + pk] = cc[ch];
+          }
           if (z > 0 && c->noise) {
             double sig = 0.0012 + 0.0019 * (z - 0.4) * (z - 0.4);
             z += sig * normal(key(c->seed, 200, k, pk));

@@ -68,6 +68,7 @@ int check_config(const vs_config* c) {
   if (c->reduce_mode < 0 || c->reduce_mode > 2) return fail(VS_ERR_ARG, "bad reduce_mode");
   for (int l = 0; l < kMaxLevels; l++)
     if (c->icp_iters[l] < 0 || c->icp_iters[l] > 100) return fail(VS_ERR_ARG, "icp_iters must be 0..100");
+  if (c->color != 0 && c->color != 1) return fail(VS_ERR_ARG, "color must be 0 or 1");
   return VS_OK;
 }
 
@@ -170,6 +171,14 @@ int reset_state(vs_session* s) {
   p.tracked = 1;
   *s->host_pose = p;
   VS_CU(cudaMemcpyAsync(s->h.pose, s->host_pose, sizeof(Pose), cudaMemcpyHostToDevice, s->stream));
+  if (s->h.col) {
+    const size_t n0 = (size_t)s->h.lv[0].W * s->h.lv[0].H;
+    VS_CU(cudaMemsetAsync(s->h.col, 0, (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2] * kBrickVox * 4, s->stream));
+    VS_CU(cudaMemsetAsync(s->h.rgb_in, 0, n0 * 3, s->stream));
+    VS_CU(cudaMemsetAsync(s->h.rgb_packed, 0, n0 * 4, s->stream));
+    for (int l = 0; l < s->h.levels; l++)
+      VS_CU(cudaMemsetAsync(s->h.m_rgb[l], 0, (size_t)s->h.lv[l].W * s->h.lv[l].H * 4, s->stream));
+  }
   // model maps start invalid (depth 0, vertex / normal -100)
   for (int l = 0; l < s->h.levels; l++) {
     size_t n = (size_t)s->h.lv[l].W * s->h.lv[l].H;
@@ -198,10 +207,11 @@ void record_frame(vs_session* s, cudaStream_t st) {
   mark(1);
   launch_icp(s->tab, h.levels, h.iters, h.reduce_mode, st, true, nullptr);
   mark(2);
-  launch_integrate(s->tab, h.tsdf_type, nullptr, nullptr, nullptr, true, st);
+  const bool color = h.col != nullptr;
+  launch_integrate(s->tab, h.tsdf_type, nullptr, nullptr, nullptr, true, st, color);
   mark(3);
   launch_raycast(s->tab, h.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
-                 nullptr, nullptr, st);
+                 nullptr, nullptr, st, LaunchShape(), nullptr, color);
   mark(4);
 }
 
@@ -253,6 +263,7 @@ void vs_config_default(vs_config* c, int width, int height) {
   c->reduce_mode = VS_REDUCE_KAHAN;
   c->tsdf_type = VS_TSDF_INT16;
   c->depth_scale = 0.001f;
+  c->color = 0;
 }
 
 const char* vs_last_error(void) { return g_err.c_str(); }
@@ -278,6 +289,10 @@ size_t vs_session_bytes(const vs_config* c) {
   b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
   for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
   b += (size_t)w * h * 4;                                                      // ray-scale map
+  if (c->color) {
+    b += (size_t)c->dim[0] * c->dim[1] * c->dim[2] * 4 + (size_t)w * h * (3 + 4);  // colour volume and frame
+    for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 4;      // colour maps
+  }
   return b;
 }
 
@@ -340,6 +355,12 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.lut_vox, (size_t)(h.dim[0] + h.dim[1] + h.dim[2]) * 4);
   rc |= alloc(s, &h.lut_ray, (size_t)(h.lv[0].W + h.lv[0].H) * 4);
   rc |= alloc(s, &h.lam_map, n0 * 4);
+  if (cfg->color) {
+    rc |= alloc(s, &h.col, nbr * kBrickVox * 4);
+    rc |= alloc(s, &h.rgb_in, n0 * 3);
+    rc |= alloc(s, &h.rgb_packed, n0 * 4);
+    for (int l = 0; l < h.levels; l++) rc |= alloc(s, &h.m_rgb[l], (size_t)h.lv[l].W * h.lv[l].H * 4);
+  }
   {
     size_t npx = 0;
     for (int l = 0; l < h.levels; l++) npx += (size_t)h.lv[l].W * h.lv[l].H;
@@ -438,7 +459,19 @@ int vs_integrate_depth(vs_session* s, const float* depth_dev, int ww, int hh, co
                        const float* T_cg_dev) {
   if (!s || !depth_dev || !T_gc_dev || !T_cg_dev) return fail(VS_ERR_ARG, "null argument");
   if (ww != s->h.lv[0].W || hh != s->h.lv[0].H) return fail(VS_ERR_ARG, "size differs from the session");
-  launch_integrate(s->tab, s->h.tsdf_type, depth_dev, T_gc_dev, T_cg_dev, false, s->stream);
+  launch_integrate(s->tab, s->h.tsdf_type, depth_dev, T_gc_dev, T_cg_dev, false, s->stream, false);
+  VS_CU(cudaGetLastError());
+  VS_CU(cudaStreamSynchronize(s->stream));
+  return VS_OK;
+}
+
+int vs_integrate_depth_color(vs_session* s, const float* depth_dev, const uint8_t* img_color_dev, int ww, int hh,
+                             const float* T_gc_dev, const float* T_cg_dev) {
+  if (!s || !depth_dev || !img_color_dev || !T_gc_dev || !T_cg_dev) return fail(VS_ERR_ARG, "null argument");
+  if (!s->h.col) return fail(VS_ERR_STATE, "session has no colour volume (cfg.color = 0)");
+  if (ww != s->h.lv[0].W || hh != s->h.lv[0].H) return fail(VS_ERR_ARG, "size differs from the session");
+  launch_pack_color(s->h, img_color_dev, s->stream);
+  launch_integrate(s->tab, s->h.tsdf_type, depth_dev, T_gc_dev, T_cg_dev, false, s->stream, true);
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
   return VS_OK;
@@ -457,6 +490,75 @@ int vs_render_maps(vs_session* s, int ww, int hh, const float* T_gc_dev, const f
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
   return VS_OK;
+}
+
+int vs_render_maps_color(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, int level, float* depth_dev, float* vtx_dev,
+                         float* nrm_dev, uint8_t* img_dev, uint8_t* rgb_dev) {
+  if (!s || !T_gc_dev || !T_cg_dev || !cam_cen || !light || !depth_dev || !vtx_dev || !nrm_dev || !rgb_dev)
+    return fail(VS_ERR_ARG, "null argument");
+  if (!s->h.col) return fail(VS_ERR_STATE, "session has no colour volume (cfg.color = 0)");
+  if (level < 0 || level >= s->h.levels) return fail(VS_ERR_ARG, "bad level");
+  if (ww != s->h.lv[level].W || hh != s->h.lv[level].H) return fail(VS_ERR_ARG, "size differs from the level");
+  VS_CU(cudaMemcpyAsync(s->dev_small, cam_cen, 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  launch_raycast(s->tab, s->h.tsdf_type, level, T_gc_dev, T_cg_dev, s->dev_small, light[0], light[1], light[2],
+                 false, depth_dev, vtx_dev, nrm_dev, img_dev, s->stream, LaunchShape(), rgb_dev, true);
+  VS_CU(cudaGetLastError());
+  VS_CU(cudaStreamSynchronize(s->stream));
+  return VS_OK;
+}
+
+int vs_set_color_frame(vs_session* s, const uint8_t* img_color, int is_host) {
+  if (!s || !img_color) return fail(VS_ERR_ARG, "null argument");
+  if (!s->h.col) return fail(VS_ERR_STATE, "session has no colour volume (cfg.color = 0)");
+  const size_t n = (size_t)s->h.lv[0].W * s->h.lv[0].H * 3;
+  VS_CU(cudaMemcpyAsync(s->h.rgb_in, img_color, n, is_host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                        s->stream));
+  VS_CU(cudaStreamSynchronize(s->stream));
+  return VS_OK;
+}
+
+static int color_transfer(vs_session* s, uint8_t* out, const uint8_t* in, int level) {
+  if (!s->h.col) return fail(VS_ERR_STATE, "session has no colour volume (cfg.color = 0)");
+  size_t n;
+  if (level < 0)
+    n = (size_t)s->h.dim[0] * s->h.dim[1] * s->h.dim[2] * 3;
+  else
+    n = (size_t)s->h.lv[level].W * s->h.lv[level].H * 3;
+  VS_CU(cudaStreamSynchronize(s->stream));
+  uint8_t* d = nullptr;
+  VS_CU(cudaMalloc(&d, n));
+  cudaError_t e = cudaSuccess;
+  if (in) {
+    e = cudaMemcpy(d, in, n, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) launch_color_volume(s->h, false, d, s->stream);
+  } else if (level < 0) {
+    launch_color_volume(s->h, true, d, s->stream);
+  } else {
+    launch_color_map_export(s->h, level, d, s->stream);
+  }
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess && out) e = cudaMemcpy(out, d, n, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "colour transfer");
+  return VS_OK;
+}
+
+int vs_get_color_volume(vs_session* s, uint8_t* rgb_host) {
+  if (!s || !rgb_host) return fail(VS_ERR_ARG, "null argument");
+  return color_transfer(s, rgb_host, nullptr, -1);
+}
+
+int vs_set_color_volume(vs_session* s, const uint8_t* rgb_host) {
+  if (!s || !rgb_host) return fail(VS_ERR_ARG, "null argument");
+  return color_transfer(s, nullptr, rgb_host, -1);
+}
+
+int vs_get_color_map(vs_session* s, int level, uint8_t* rgb_host) {
+  if (!s || !rgb_host) return fail(VS_ERR_ARG, "null argument");
+  if (level < 0 || level >= s->h.levels) return fail(VS_ERR_ARG, "bad level");
+  return color_transfer(s, rgb_host, nullptr, level);
 }
 
 // ---- per-frame path --------------------------------------------------------
@@ -505,14 +607,14 @@ int vs_stage_track(vs_session* s) {
 }
 int vs_stage_integrate(vs_session* s) {
   if (!s) return fail(VS_ERR_ARG, "null session");
-  launch_integrate(s->tab, s->h.tsdf_type, nullptr, nullptr, nullptr, true, s->stream);
+  launch_integrate(s->tab, s->h.tsdf_type, nullptr, nullptr, nullptr, true, s->stream, s->h.col != nullptr);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }
 int vs_stage_raycast(vs_session* s) {
   if (!s) return fail(VS_ERR_ARG, "null session");
   launch_raycast(s->tab, s->h.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
-                 nullptr, nullptr, s->stream);
+                 nullptr, nullptr, s->stream, LaunchShape(), nullptr, s->h.col != nullptr);
   VS_CU(cudaGetLastError());
   return VS_OK;
 }

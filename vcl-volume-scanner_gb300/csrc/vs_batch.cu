@@ -35,9 +35,10 @@ struct Schedule {
   int reduce_mode = -1;
   int tsdf_type = -1;
   int timing = 0;
+  int color = 0;  // some session keeps a colour volume
   bool covers(const Schedule& o) const {
     if (o.reduce_mode != reduce_mode || o.tsdf_type != tsdf_type || o.timing != timing) return false;
-    if (o.levels > levels || (o.inmaps && !inmaps)) return false;
+    if (o.levels > levels || (o.inmaps && !inmaps) || (o.color && !color)) return false;
     for (int l = 0; l < kMaxLevels; l++)
       if (o.iters[l] > iters[l]) return false;
     return true;
@@ -86,10 +87,10 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
   mark(1);
   launch_icp(b->d_tab, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
   mark(2);
-  launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st);
+  launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
   mark(3);
   launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
-                 nullptr, nullptr, st, b->shape);
+                 nullptr, nullptr, st, b->shape, nullptr, k.color != 0);
   mark(4);
   launch_gather_heads(b->d_tab, b->d_heads, st);
   cudaMemcpyAsync(b->h_heads[r], b->d_heads, kMaxSlots * kPoseHeadBytes, cudaMemcpyDeviceToHost, st);
@@ -143,6 +144,7 @@ int check_sessions(vs_batch* b, vs_session* const* ss, int n, Schedule& k) {
     for (int l = 0; l < h.levels; l++)
       if (h.iters[l] > k.iters[l]) k.iters[l] = h.iters[l];
     if (h.cos_normal > -2.0f) k.inmaps = 1;
+    if (h.col) k.color = 1;
   }
   k.timing = b->timing ? 1 : 0;
   return VS_OK;
@@ -156,6 +158,7 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
         b->sched.timing == k.timing) {
       m.levels = std::max(m.levels, b->sched.levels);
       m.inmaps |= b->sched.inmaps;
+      m.color |= b->sched.color;
       for (int l = 0; l < kMaxLevels; l++) m.iters[l] = std::max(m.iters[l], b->sched.iters[l]);
     }
     // the graphs read both ring buffers: let in-flight steps finish first
@@ -421,7 +424,7 @@ int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps,
       for (int r = 0; r <= reps && e == cudaSuccess; r++) {
         if (r == 1) e = cudaEventRecord(e0, b->stream);
         launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr,
-                       nullptr, nullptr, nullptr, b->stream, sh);
+                       nullptr, nullptr, nullptr, b->stream, sh, nullptr, k.color != 0);
         if (e == cudaSuccess) e = cudaGetLastError();
       }
       if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);

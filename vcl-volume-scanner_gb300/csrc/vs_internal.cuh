@@ -93,6 +93,11 @@ struct SessionDev {
   float* lut_vox;                // voxel centre coordinate per axis: dim[0] + dim[1] + dim[2]
   float* lut_ray;                // level-0 K^-1 [x 1 1] (W) then [1 y 1] (H) components
   float4* ray_hit;               // ray-cast surface points, every level's pixels in turn
+  // colour (NULL pointers when the session keeps none)
+  uint32_t* col;                 // colour bricks parallel to vol: per voxel 0x00BBGGRR
+  uint8_t* rgb_in;               // level-0 colour frame, planar R, G, B
+  uint32_t* rgb_packed;          // the same frame as one 0x00BBGGRR word per pixel
+  uint32_t* m_rgb[kMaxLevels];   // ray-cast colour per pixel, 0x00BBGGRR
   float* lam_map;                // level-0 ray scale per pixel (NULL: computed per voxel)
 };
 
@@ -193,6 +198,9 @@ __device__ inline F3 pos_in_world(F3 v, const SessionDev& s) {
 // Bricks are 512 consecutive words, x fastest inside the brick; bricks are
 // ordered x fastest, then y, then z.
 // ---------------------------------------------------------------------------
+__host__ __device__ inline uint32_t pack_rgb(uint32_t r, uint32_t g, uint32_t b) { return r | (g << 8) | (b << 16); }
+__host__ __device__ inline uint32_t rgb_channel(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
+
 // occupancy cell index of brick (bx, by, bz) at level `shift` (2: 4^3
 // bricks, 4: 16^3 bricks) in a grid of nc cells per axis
 __host__ __device__ inline uint32_t occ_cell(int bx, int by, int bz, int shift, const int* nc) {
@@ -280,16 +288,23 @@ void launch_bilateral_float(const SessionDev& h, const float* in, float* out, cu
 void launch_icp(const BatchTable* bt, int max_levels, const int* max_iters, int reduce_mode, cudaStream_t st,
                 bool frame_mode, const float* init_T12_dev);
 // depth / Tgc / Tcg: explicit inputs of a one-slot table, or NULL for each
-// session's own level-0 depth and pose
+// session's own level-0 depth and pose; color: run the variant that also
+// blends the colour of sessions that keep a colour volume
 void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc,
-                      const float* Tcg, bool gate_on_tracking, cudaStream_t st);
+                      const float* Tcg, bool gate_on_tracking, cudaStream_t st, bool color = false);
 // level < 0: every level of every slot into the sessions' model maps; else
-// one level of a one-slot table into the external outputs with explicit poses
+// one level of a one-slot table into the external outputs with explicit poses;
+// color: the shading variant that also interpolates colour
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate_on_tracking, float* out_depth,
                     float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st,
-                    const LaunchShape& shape = LaunchShape());
+                    const LaunchShape& shape = LaunchShape(), uint8_t* out_rgb = nullptr, bool color = false);
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st);
+// planar colour frame -> one word per pixel (rgb: a device frame, or NULL for the session's own)
+void launch_pack_color(const SessionDev& h, const uint8_t* rgb, cudaStream_t st);
+// colour volume <-> reference layout (three planes of x-fastest bytes)
+void launch_color_volume(const SessionDev& h, bool do_export, uint8_t* planes, cudaStream_t st);
+void launch_color_map_export(const SessionDev& h, int level, uint8_t* planes, cudaStream_t st);
 void launch_volume_init(const SessionDev& h, cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
 // pose heads of every slot, kPoseHeadBytes each, into out (kMaxSlots slots)

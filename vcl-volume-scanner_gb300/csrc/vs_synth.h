@@ -30,6 +30,11 @@ void vs_synth_default(vs_synth_config* c, int width, int height);
  * global frame (3).  T_gc / centre_cam0 may be NULL.  Returns 0 on success. */
 int vs_synth_generate(const vs_synth_config* c, uint16_t* depth, double* T_gc,
                       double* centre_cam0);
+/* the same plus a registered colour image per frame: rgb is
+ * n_frames * 3 * height * width uint8, planar R, G, B per frame (a smooth
+ * texture of the true surface point; 0 where the ray hits nothing) */
+int vs_synth_generate_rgb(const vs_synth_config* c, uint16_t* depth, uint8_t* rgb, double* T_gc,
+                          double* centre_cam0);
 
 #ifdef __cplusplus
 }

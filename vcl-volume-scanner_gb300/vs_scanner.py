@@ -55,6 +55,7 @@ class VsConfig(ctypes.Structure):
         ("reduce_mode", ctypes.c_int),
         ("tsdf_type", ctypes.c_int),
         ("depth_scale", ctypes.c_float),
+        ("color", ctypes.c_int),
     ]
 
 
@@ -148,6 +149,12 @@ _SIGS = {
     "vs_kernels_per_frame": (_I, [ctypes.POINTER(VsConfig)]),
     "vs_get_input_raw": (_I, [_P, _P]),
     "vs_get_device_buffer": (_I, [_P, _I, ctypes.POINTER(_P)]),
+    "vs_integrate_depth_color": (_I, [_P, _P, _P, _I, _I, _P, _P]),
+    "vs_render_maps_color": (_I, [_P, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
+    "vs_set_color_frame": (_I, [_P, _P, _I]),
+    "vs_get_color_volume": (_I, [_P, _P]),
+    "vs_set_color_volume": (_I, [_P, _P]),
+    "vs_get_color_map": (_I, [_P, _I, _P]),
     "vs_integrate_depth_noalloc": (_I, [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _I, _I, _P,
                                         _P, _P, _P]),
     "vs_batch_create": (_I, [ctypes.POINTER(_P)]),
@@ -200,6 +207,8 @@ def load_synth(path=SYNTH_PATH):
         lib.vs_synth_default.argtypes = [ctypes.POINTER(SynthConfig), _I, _I]
         lib.vs_synth_generate.restype = _I
         lib.vs_synth_generate.argtypes = [ctypes.POINTER(SynthConfig), _P, _P, _P]
+        lib.vs_synth_generate_rgb.restype = _I
+        lib.vs_synth_generate_rgb.argtypes = [ctypes.POINTER(SynthConfig), _P, _P, _P, _P]
         _synth = lib
     return _synth
 
@@ -297,6 +306,43 @@ class Session:
     def cdtoc_convert_depth_to_tsdf(self, depth_dev, T_gc_dev, T_cg_dev):
         _check(self.lib.vs_integrate_depth(self.h, _ptr(depth_dev), self.cfg.width, self.cfg.height,
                                            _ptr(T_gc_dev), _ptr(T_cg_dev)))
+
+    def cdtocc_convert_depth_to_tsdf_color(self, depth_dev, rgb_dev, T_gc_dev, T_cg_dev):
+        _check(self.lib.vs_integrate_depth_color(self.h, _ptr(depth_dev), _ptr(rgb_dev), self.cfg.width,
+                                                 self.cfg.height, _ptr(T_gc_dev), _ptr(T_cg_dev)))
+
+    def rmi_render_maps_color(self, level, T_gc_dev, T_cg_dev, cam_cen, light, depth_dev, vertex_dev, normal_dev,
+                              img_dev, rgb_dev):
+        w, h = self.levels[level][0], self.levels[level][1]
+        c = np.ascontiguousarray(cam_cen, dtype=np.float32)
+        l = np.ascontiguousarray(light, dtype=np.float32)
+        _check(self.lib.vs_render_maps_color(self.h, w, h, _ptr(T_gc_dev), _ptr(T_cg_dev), _ptr(c), _ptr(l), level,
+                                             _ptr(depth_dev), _ptr(vertex_dev), _ptr(normal_dev), _ptr(img_dev),
+                                             _ptr(rgb_dev)))
+
+    def set_color_frame(self, rgb):
+        """planar uint8 (3, height, width) host array, or a device pointer (int)"""
+        if isinstance(rgb, int):
+            _check(self.lib.vs_set_color_frame(self.h, _ptr(rgb), 0))
+        else:
+            c = np.ascontiguousarray(rgb, dtype=np.uint8)
+            _check(self.lib.vs_set_color_frame(self.h, _ptr(c), 1))
+
+    def color_volume(self):
+        n = self.cfg.dim[0] * self.cfg.dim[1] * self.cfg.dim[2]
+        out = np.empty(3 * n, np.uint8)
+        _check(self.lib.vs_get_color_volume(self.h, _ptr(out)))
+        return out.reshape(3, n)
+
+    def set_color_volume(self, rgb):
+        c = np.ascontiguousarray(rgb, dtype=np.uint8)
+        _check(self.lib.vs_set_color_volume(self.h, _ptr(c)))
+
+    def color_map(self, level):
+        w, h = self.levels[level][0], self.levels[level][1]
+        out = np.empty((3, h, w), np.uint8)
+        _check(self.lib.vs_get_color_map(self.h, level, _ptr(out)))
+        return out
 
     def rmi_render_maps_for_icp(self, level, T_gc_dev, T_cg_dev, cam_cen, light, depth_dev, vertex_dev,
                                 normal_dev, img_dev):
@@ -608,6 +654,19 @@ def synth_generate(cfg):
     if rc != 0:
         raise ValueError("bad synth config")
     return depth, T, c
+
+
+def synth_generate_rgb(cfg):
+    """(depth uint16 [n,h,w], rgb uint8 [n,3,h,w] planar, T_gc [n,4,4], scene centre)"""
+    n, h, w = cfg.n_frames, cfg.height, cfg.width
+    depth = np.empty((n, h, w), np.uint16)
+    rgb = np.empty((n, 3, h, w), np.uint8)
+    T = np.empty((n, 4, 4), np.float64)
+    c = np.empty(3, np.float64)
+    rc = load_synth().vs_synth_generate_rgb(ctypes.byref(cfg), _ptr(depth), _ptr(rgb), _ptr(T), _ptr(c))
+    if rc != 0:
+        raise ValueError("bad synth config")
+    return depth, rgb, T, c
 
 
 def cube_around(centre, size, dim):
