@@ -211,6 +211,37 @@ int vs_get_active_bricks(vs_session* s, uint32_t* count, uint32_t* bricks_host,
 int vs_get_maps(vs_session* s, int level, float* model_depth, float* model_vertex3,
                 float* model_normal3, uint8_t* model_img, float* input_depth,
                 float* input_vertex3, float* input_normal3);
+/* ---- snapshot / resume ---------------------------------------------------
+ * The reference saves scans through a closed KAISION writer (.vcl,
+ * z_yooji_object_scanner.cpp:2732-2745) and moves the cube with
+ * to_host / from_host (_yooji_cuda_object_cube.hpp:6-85).  The snapshot here
+ * is this library's own file: "VSSNAP01", the vs_config, the FP64 pose and
+ * frame count, then only the sub-cubes holding data (index list, their TSDF
+ * words, and their colour words when the session keeps colour).  Loading
+ * creates a session, restores volume, occupancy and pose, and ray-casts the
+ * model maps, so the next frame continues exactly as the saved session
+ * would. */
+int vs_session_save(vs_session* s, const char* path);
+/* the configuration a session was created with (e.g. after vs_session_load) */
+int vs_session_config(vs_session* s, vs_config* out);
+int vs_session_load(const char* path, vs_session** out);
+
+/* ---- surface extraction ---------------------------------------------------
+ * The zero level set of the TSDF as a triangle soup, by marching tetrahedra:
+ * every cell of 2x2x2 voxels whose eight corners have weight > 0 is split
+ * into six tetrahedra around its (0,0,0)-(1,1,1) diagonal; a vertex is the
+ * linear zero crossing on a tetrahedron edge, in world coordinates, and each
+ * triangle faces positive TSDF (free space).  xyz: 9 floats per triangle;
+ * rgb (may be NULL; sessions with colour): 9 bytes per triangle, the edge's
+ * two voxel colours mixed with the same weights and rounded.  Writes at most
+ * capacity triangles and returns the total in *n_triangles (call again with a
+ * larger buffer when it exceeds capacity).  Host buffers; the order of the
+ * triangles is not fixed. */
+int vs_extract_mesh(vs_session* s, float* xyz_host, uint8_t* rgb_host, uint64_t capacity, uint64_t* n_triangles);
+/* the same mesh written as a binary little-endian PLY (vertex x y z [r g b],
+ * face vertex_indices) */
+int vs_save_mesh_ply(vs_session* s, const char* path);
+
 /* ---- instrumentation (the reference prints per-stage stopwatch times,
  * z_yooji_object_scanner.cpp:489-604) ------------------------------------- */
 

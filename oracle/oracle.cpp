@@ -1220,6 +1220,96 @@ void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> ca
 }
 
 // ---------------------------------------------------------------------------
+// surface extraction: marching tetrahedra over the cells whose eight corners
+// have weight > 0; six tetrahedra around the (0,0,0)-(1,1,1) diagonal; a vertex
+// is the linear zero crossing on an edge, in world coordinates; triangles face
+// the positive side; colour mixed along the edge with the same weight and
+// rounded (half up).  Same operations and corner order as the CUDA kernel.
+// ---------------------------------------------------------------------------
+template <class T>
+uint64_t extract_mesh(const Volume<T>& V, float* xyz, uint8_t* rgb, uint64_t capacity) {
+  static const int tet[6][4] = {{0, 7, 1, 3}, {0, 7, 3, 2}, {0, 7, 2, 6}, {0, 7, 6, 4}, {0, 7, 4, 5}, {0, 7, 5, 1}};
+  const Cfg<T>& g = V.g;
+  const int X = g.dim[0], Y = g.dim[1], Z = g.dim[2];
+  const size_t n3 = (size_t)X * Y * Z;
+  uint64_t count = 0;
+  struct EV {
+    V3<T> p;
+    T c[3];
+  };
+  auto emit = [&](const EV& a, const EV& b, const EV& c, V3<T> ci, V3<T> co) {
+    V3<T> u = b.p - a.p, v = c.p - a.p;
+    V3<T> n = v3(u.y * v.z - u.z * v.y, u.z * v.x - u.x * v.z, u.x * v.y - u.y * v.x);
+    V3<T> d = co - ci;
+    bool flip = (n.x * d.x + n.y * d.y + n.z * d.z) < T(0);
+    const EV* t[3] = {&a, flip ? &c : &b, flip ? &b : &c};
+    if (count < capacity) {
+      for (int k = 0; k < 3; k++) {
+        xyz[9 * count + 3 * k] = (float)t[k]->p.x;
+        xyz[9 * count + 3 * k + 1] = (float)t[k]->p.y;
+        xyz[9 * count + 3 * k + 2] = (float)t[k]->p.z;
+        if (rgb)
+          for (int ch = 0; ch < 3; ch++)
+            rgb[9 * count + 3 * k + ch] = (uint8_t)std::fmin(T(255.0f), std::fmax(T(0), t[k]->c[ch] + T(0.5f)));
+      }
+    }
+    count++;
+  };
+  for (int z = 0; z + 1 < Z; z++)
+    for (int y = 0; y + 1 < Y; y++)
+      for (int x = 0; x + 1 < X; x++) {
+        T v[8], col[8][3];
+        bool ok = true;
+        for (int c = 0; c < 8 && ok; c++) {
+          size_t idx = ((size_t)(z + (c >> 2)) * Y + (y + ((c >> 1) & 1))) * X + (x + (c & 1));
+          ok = V.w[idx] != 0;
+          v[c] = V.tsdf[idx];
+          for (int k = 0; k < 3; k++) col[c][k] = V.col.empty() ? T(0) : (T)V.col[idx + k * n3];
+        }
+        if (!ok) continue;
+        unsigned neg = 0;
+        for (int c = 0; c < 8; c++) neg |= (v[c] < T(0) ? 1u : 0u) << c;
+        if (neg == 0u || neg == 0xffu) continue;
+        auto P = [&](int c) { return v3<T>((T)(x + (c & 1)), (T)(y + ((c >> 1) & 1)), (T)(z + (c >> 2))); };
+        auto E = [&](int a, int c) {
+          T t = (T(0) - v[a]) / (v[c] - v[a]);
+          V3<T> pa = P(a), pb = P(c);
+          V3<T> pv = v3(pa.x + t * (pb.x - pa.x), pa.y + t * (pb.y - pa.y), pa.z + t * (pb.z - pa.z));
+          EV e;
+          e.p = pos_in_world(pv, g.origin, g.vox_inv);
+          for (int k = 0; k < 3; k++) e.c[k] = col[a][k] + t * (col[c][k] - col[a][k]);
+          return e;
+        };
+        for (int t = 0; t < 6; t++) {
+          int in[4], out[4], ni = 0, no = 0;
+          for (int k = 0; k < 4; k++) {
+            int c = tet[t][k];
+            if ((neg >> c) & 1u)
+              in[ni++] = c;
+            else
+              out[no++] = c;
+          }
+          if (ni == 0 || no == 0) continue;
+          V3<T> ci = v3<T>(0, 0, 0), co = v3<T>(0, 0, 0);
+          for (int k = 0; k < ni; k++) ci = ci + P(in[k]);
+          for (int k = 0; k < no; k++) co = co + P(out[k]);
+          ci = (T(1) / (T)ni) * ci;
+          co = (T(1) / (T)no) * co;
+          if (ni == 1 || no == 1) {
+            int lone = (ni == 1) ? in[0] : out[0];
+            const int* rest = (ni == 1) ? out : in;
+            emit(E(lone, rest[0]), E(lone, rest[1]), E(lone, rest[2]), ci, co);
+          } else {
+            EV e00 = E(in[0], out[0]), e01 = E(in[0], out[1]), e11 = E(in[1], out[1]), e10 = E(in[1], out[0]);
+            emit(e00, e01, e11, ci, co);
+            emit(e00, e11, e10, ci, co);
+          }
+        }
+      }
+  return count;
+}
+
+// ---------------------------------------------------------------------------
 // session: so_Scan_Object hot path (z_yooji_object_scanner.cpp:472-629)
 // ---------------------------------------------------------------------------
 template <class T>
@@ -1426,6 +1516,9 @@ void or_raycast_color(const or_volume* v, int level, const float* T_gc, const fl
                       const float* light, float* depth, float* vtx3, float* nrm3, uint8_t* img, uint8_t* rgb) {
   raycast<float>(v->v, level, T_gc, T_cg, v3(cam_cen[0], cam_cen[1], cam_cen[2]),
                  v3(light[0], light[1], light[2]), depth, vtx3, nrm3, img, rgb);
+}
+uint64_t or_extract_mesh(const or_volume* v, float* xyz, uint8_t* rgb, uint64_t capacity) {
+  return extract_mesh<float>(v->v, xyz, rgb, capacity);
 }
 void or_raycast(const or_volume* v, int level, const float* T_gc, const float* T_cg,
                 const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,

@@ -77,6 +77,7 @@ def load():
             "or_volume_get_color": (None, [P, P]),
             "or_volume_set_color": (None, [P, P]),
             "or_raycast_color": (None, [P, I, P, P, P, P, P, P, P, P, P]),
+            "or_extract_mesh": (ctypes.c_uint64, [P, P, P, ctypes.c_uint64]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
             "or_session_destroy": (None, [P]),
@@ -311,6 +312,13 @@ class Volume:
         c = np.ascontiguousarray(rgb, np.uint8)
         assert c.size == 3 * self.n
         self.lib.or_volume_set_color(self.h, _p(c))
+
+    def mesh(self, with_color=False):
+        n = self.lib.or_extract_mesh(self.h, None, None, 0)
+        xyz = np.empty((max(n, 1), 3, 3), np.float32)
+        rgb = np.empty((max(n, 1), 3, 3), np.uint8) if with_color else None
+        self.lib.or_extract_mesh(self.h, _p(xyz), _p(rgb) if with_color else None, n)
+        return xyz[:n], (rgb[:n] if with_color else None)
 
     def raycast_color(self, level, T_gc, T_cg, cam, light=(0.0, 0.0, -1.0)):
         w, h = level_sizes(self.cfg)[level]

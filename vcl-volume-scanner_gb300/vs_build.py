@@ -20,8 +20,8 @@ NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 CXX = os.environ.get("CXX", "g++")
 
 CU_SOURCES = [
-    "k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "vs_api.cu", "vs_batch.cu", "vs_server.cu",
-    "vs_noalloc.cu",
+    "k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "k_mesh.cu", "vs_api.cu", "vs_batch.cu",
+    "vs_server.cu", "vs_snapshot.cu", "vs_noalloc.cu",
 ]
 HEADERS = ["vs_internal.cuh", "vs_host.h"]
 NVCC_FLAGS = [

@@ -155,6 +155,11 @@ _SIGS = {
     "vs_get_color_volume": (_I, [_P, _P]),
     "vs_set_color_volume": (_I, [_P, _P]),
     "vs_get_color_map": (_I, [_P, _I, _P]),
+    "vs_session_save": (_I, [_P, ctypes.c_char_p]),
+    "vs_session_load": (_I, [ctypes.c_char_p, ctypes.POINTER(_P)]),
+    "vs_session_config": (_I, [_P, ctypes.POINTER(VsConfig)]),
+    "vs_extract_mesh": (_I, [_P, _P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
+    "vs_save_mesh_ply": (_I, [_P, ctypes.c_char_p]),
     "vs_integrate_depth_noalloc": (_I, [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _I, _I, _P,
                                         _P, _P, _P]),
     "vs_batch_create": (_I, [ctypes.POINTER(_P)]),
@@ -262,13 +267,42 @@ def level_intrinsics(cfg):
 class Session:
     """One scanning session: volume, pose, frame pyramid and model maps on the device."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, _handle=None):
         self.lib = load()
-        self.cfg = cfg
         h = ctypes.c_void_p()
-        _check(self.lib.vs_session_create(ctypes.byref(cfg), ctypes.byref(h)))
+        if _handle is None:
+            _check(self.lib.vs_session_create(ctypes.byref(cfg), ctypes.byref(h)))
+        else:
+            h = _handle
+            cfg = VsConfig()
+            _check(self.lib.vs_session_config(h, ctypes.byref(cfg)))
+        self.cfg = cfg
         self.h = h
         self.levels = level_intrinsics(cfg)
+
+    @classmethod
+    def load(cls, path):
+        """a session resumed from a snapshot written by save()"""
+        h = ctypes.c_void_p()
+        _check(load().vs_session_load(os.fsencode(path), ctypes.byref(h)))
+        return cls(None, _handle=h)
+
+    def save(self, path):
+        _check(self.lib.vs_session_save(self.h, os.fsencode(path)))
+
+    def mesh(self, with_color=False):
+        """triangle soup of the zero level set: (xyz [n,3,3] float32, rgb [n,3,3] uint8 or None)"""
+        n = ctypes.c_uint64(0)
+        _check(self.lib.vs_extract_mesh(self.h, None, None, 0, ctypes.byref(n)))
+        cap = n.value
+        xyz = np.empty((max(cap, 1), 3, 3), np.float32)
+        rgb = np.empty((max(cap, 1), 3, 3), np.uint8) if with_color else None
+        _check(self.lib.vs_extract_mesh(self.h, _ptr(xyz), _ptr(rgb), cap, ctypes.byref(n)))
+        m = min(cap, n.value)
+        return xyz[:m], (rgb[:m] if with_color else None)
+
+    def save_mesh_ply(self, path):
+        _check(self.lib.vs_save_mesh_ply(self.h, os.fsencode(path)))
 
     def close(self):
         if self.h:
