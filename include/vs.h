@@ -167,6 +167,25 @@ int vs_set_color_volume(vs_session* s, const uint8_t* rgb_host);
 /* the colour image of the last frame's ray-cast at a level, planar */
 int vs_get_color_map(vs_session* s, int level, uint8_t* rgb_host);
 
+/* ---- depth -> colour camera registration ------------------------------------
+ * z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates
+ * (z_yooji_object_scanner.cpp:2429-2476): the depth map as seen from a second
+ * (colour) camera, for rigs whose colour camera is not the depth camera.  Each
+ * depth pixel with depth d > 0 is back-projected with K_d, moved by the 4x4
+ * depth-to-colour transform T_rgb_wrt_d (row-major, metres), projected with
+ * K_rgb and rounded (half away from zero); a colour pixel keeps the smallest
+ * depth landing on it, 0 where none does.  K_*: host {fx, fy, cx, cy};
+ * T_rgb_wrt_d: host float[16]; buffers on the device; asynchronous on stream.
+ * The result (colour-camera depth, registered to the colour image) can feed
+ * a session configured with the colour camera's intrinsics. */
+int vs_warp_depth_to_color(const float* depth_dev, int w_d, int h_d, const float* K_d, const float* T_rgb_wrt_d,
+                           const float* K_rgb, int w_rgb, int h_rgb, float* depth_rgb_dev, void* stream);
+/* the same on uint16 depth units (depth_scale: units -> metres), giving a
+ * uint16 frame for vs_scan_frame */
+int vs_warp_depth_mm_to_color(const uint16_t* depth_mm_dev, int w_d, int h_d, float depth_scale, const float* K_d,
+                              const float* T_rgb_wrt_d, const float* K_rgb, int w_rgb, int h_rgb,
+                              uint16_t* depth_mm_rgb_dev, void* stream);
+
 /* ---- per-frame hot path (so_Scan_Object) -------------------------------- */
 
 /* One frame on device input, asynchronous on `stream` (cudaStream_t, NULL =

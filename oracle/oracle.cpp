@@ -1517,6 +1517,27 @@ void or_raycast_color(const or_volume* v, int level, const float* T_gc, const fl
   raycast<float>(v->v, level, T_gc, T_cg, v3(cam_cen[0], cam_cen[1], cam_cen[2]),
                  v3(light[0], light[1], light[2]), depth, vtx3, nrm3, img, rgb);
 }
+// z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates
+// (z_yooji_object_scanner.cpp:2429-2476), raster order, z-buffer keeping the
+// smaller depth; NaN projections are dropped (the reference's ROUNDF of NaN is
+// undefined)
+void or_warp_depth(const float* depth, int wd, int hd, const float* Kd, const float* T, const float* Kr, int wr,
+                   int hr, float* out) {
+  for (int i = 0; i < wr * hr; i++) out[i] = 0.0f;
+  for (int j = 0; j < hd; j++)
+    for (int i = 0; i < wd; i++) {
+      float td = depth[(size_t)j * wd + i];
+      if (!(td > 0.0f)) continue;
+      V3<float> p = transform(back_project((float)i, (float)j, Kd, td), T);
+      float u, v;
+      project(p, Kr, u, v);
+      if (std::isnan(u) || std::isnan(v)) continue;
+      int tx = roundf_ref(u), ty = roundf_ref(v);
+      if (tx < 0 || tx > wr - 1 || ty < 0 || ty > hr - 1) continue;
+      float& cur = out[(size_t)ty * wr + tx];
+      if (cur > td || cur <= 0.0f) cur = td;
+    }
+}
 uint64_t or_extract_mesh(const or_volume* v, float* xyz, uint8_t* rgb, uint64_t capacity) {
   return extract_mesh<float>(v->v, xyz, rgb, capacity);
 }

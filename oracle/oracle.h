@@ -110,6 +110,9 @@ void or_volume_set_color(or_volume* v, const uint8_t* rgb);
 void or_raycast_color(const or_volume* v, int level, const float* T_gc, const float* T_cg,
                       const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,
                       uint8_t* img, uint8_t* rgb);
+/* depth map seen from a second camera (z-buffer, smaller depth wins) */
+void or_warp_depth(const float* depth, int wd, int hd, const float* Kd, const float* T, const float* Kr, int wr,
+                   int hr, float* out);
 /* marching-tetrahedra mesh of the zero level set (9 floats / 9 colour bytes
  * per triangle, at most capacity written); returns the triangle count */
 uint64_t or_extract_mesh(const or_volume* v, float* xyz, uint8_t* rgb, uint64_t capacity);

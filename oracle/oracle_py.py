@@ -78,6 +78,7 @@ def load():
             "or_volume_set_color": (None, [P, P]),
             "or_raycast_color": (None, [P, I, P, P, P, P, P, P, P, P, P]),
             "or_extract_mesh": (ctypes.c_uint64, [P, P, P, ctypes.c_uint64]),
+            "or_warp_depth": (None, [P, I, I, P, P, P, I, I, P]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
             "or_session_destroy": (None, [P]),
@@ -158,6 +159,16 @@ def level_K(cfg):
     out = np.zeros(12, np.float32)
     load().or_level_intrinsics(_p(K0), 3, _p(out))
     return out.reshape(3, 4)
+
+
+def warp_depth(depth_m, Kd, T_rgb_wrt_d, Kr, wr, hr):
+    """depth seen from the colour camera (z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates)"""
+    d = np.ascontiguousarray(depth_m, np.float32)
+    hd, wd = d.shape
+    out = np.empty((hr, wr), np.float32)
+    load().or_warp_depth(_p(d), wd, hd, _p(np.asarray(Kd, np.float32)), _p(np.asarray(T_rgb_wrt_d, np.float32).ravel()),
+                         _p(np.asarray(Kr, np.float32)), wr, hr, _p(out))
+    return out
 
 
 def depth_to_m(mm, scale=0.001):

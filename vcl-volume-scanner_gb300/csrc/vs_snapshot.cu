@@ -1,5 +1,6 @@
 // Snapshot / resume and mesh export (vs_session_save / vs_session_load,
-// vs_extract_mesh, vs_save_mesh_ply in include/vs.h).
+// vs_extract_mesh, vs_save_mesh_ply in include/vs.h), and the host side of the
+// depth -> colour registration (vs_warp_depth_*).
 //
 // Snapshot file (little-endian, this library's own format; the reference's
 // .vcl writer is closed):
@@ -33,6 +34,9 @@ void launch_mesh(const SessionDev& h, const SessionDev* d, const uint32_t* brick
                  uint64_t capacity, unsigned long long* count, cudaStream_t st);
 void launch_bricks_copy(const SessionDev& h, const uint32_t* bricks, int n, void* packed_vol, uint32_t* packed_col,
                         bool to_packed, cudaStream_t st);
+template <class T>
+void launch_warp_depth(const T* in, int wd, int hd, const float* Kd, const float* T_rgb_d, const float* Kr, int wr,
+                       int hr, float scale, unsigned* scratch, T* out, cudaStream_t st);
 }  // namespace vs
 
 using namespace vs;
@@ -251,6 +255,53 @@ int vs_save_mesh_ply(vs_session* s, const char* path) {
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) return fail_code(VS_ERR_ARG, std::string("write failed: ") + path);
   return VS_OK;
+}
+
+}  // extern "C"
+
+// ---- depth -> colour registration (k_register.cu) ----------------------------
+
+static int warp_checks(const void* in, int wd, int hd, const float* Kd, const float* T, const float* Kr, int wr,
+                       int hr, const void* out) {
+  if (!in || !Kd || !T || !Kr || !out) return fail_code(VS_ERR_ARG, "null argument");
+  if (wd < 1 || hd < 1 || wr < 1 || hr < 1 || wd > 8192 || hd > 8192 || wr > 8192 || hr > 8192)
+    return fail_code(VS_ERR_ARG, "image size out of range (1..8192)");
+  if (Kd[0] == 0 || Kd[1] == 0 || Kr[0] == 0 || Kr[1] == 0) return fail_code(VS_ERR_ARG, "focal length is zero");
+  return VS_OK;
+}
+
+template <class T>
+static int warp_run(const T* in, int wd, int hd, const float* Kd, const float* Tm, const float* Kr, int wr, int hr,
+                    float scale, T* out, void* stream) {
+  unsigned* scratch = nullptr;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&scratch), (size_t)wr * hr * 4, st);
+  if (e != cudaSuccess) return cuda_fail_code(e, "warp scratch");
+  launch_warp_depth<T>(in, wd, hd, Kd, Tm, Kr, wr, hr, scale, scratch, out, st);
+  e = cudaGetLastError();
+  cudaError_t e2 = cudaFreeAsync(scratch, st);
+  if (e == cudaSuccess) e = e2;
+  if (e != cudaSuccess) return cuda_fail_code(e, "depth warp");
+  return VS_OK;
+}
+
+extern "C" {
+
+int vs_warp_depth_to_color(const float* depth_dev, int w_d, int h_d, const float* K_d, const float* T_rgb_wrt_d,
+                           const float* K_rgb, int w_rgb, int h_rgb, float* depth_rgb_dev, void* stream) {
+  int rc = warp_checks(depth_dev, w_d, h_d, K_d, T_rgb_wrt_d, K_rgb, w_rgb, h_rgb, depth_rgb_dev);
+  if (rc) return rc;
+  return warp_run<float>(depth_dev, w_d, h_d, K_d, T_rgb_wrt_d, K_rgb, w_rgb, h_rgb, 1.0f, depth_rgb_dev, stream);
+}
+
+int vs_warp_depth_mm_to_color(const uint16_t* depth_mm_dev, int w_d, int h_d, float depth_scale, const float* K_d,
+                              const float* T_rgb_wrt_d, const float* K_rgb, int w_rgb, int h_rgb,
+                              uint16_t* depth_mm_rgb_dev, void* stream) {
+  int rc = warp_checks(depth_mm_dev, w_d, h_d, K_d, T_rgb_wrt_d, K_rgb, w_rgb, h_rgb, depth_mm_rgb_dev);
+  if (rc) return rc;
+  if (!(depth_scale > 0)) return fail_code(VS_ERR_ARG, "depth_scale must be > 0");
+  return warp_run<uint16_t>(depth_mm_dev, w_d, h_d, K_d, T_rgb_wrt_d, K_rgb, w_rgb, h_rgb, depth_scale,
+                            depth_mm_rgb_dev, stream);
 }
 
 }  // extern "C"

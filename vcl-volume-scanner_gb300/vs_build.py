@@ -21,7 +21,7 @@ CXX = os.environ.get("CXX", "g++")
 
 CU_SOURCES = [
     "k_filter.cu", "k_icp.cu", "k_integrate.cu", "k_raycast.cu", "k_mesh.cu", "vs_api.cu", "vs_batch.cu",
-    "vs_server.cu", "vs_snapshot.cu", "vs_noalloc.cu",
+    "vs_server.cu", "vs_snapshot.cu", "vs_noalloc.cu", "k_register.cu",
 ]
 HEADERS = ["vs_internal.cuh", "vs_host.h"]
 NVCC_FLAGS = [

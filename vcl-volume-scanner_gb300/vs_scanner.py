@@ -160,6 +160,8 @@ _SIGS = {
     "vs_session_config": (_I, [_P, ctypes.POINTER(VsConfig)]),
     "vs_extract_mesh": (_I, [_P, _P, _P, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]),
     "vs_save_mesh_ply": (_I, [_P, ctypes.c_char_p]),
+    "vs_warp_depth_to_color": (_I, [_P, _I, _I, _P, _P, _P, _I, _I, _P, _P]),
+    "vs_warp_depth_mm_to_color": (_I, [_P, _I, _I, ctypes.c_float, _P, _P, _P, _I, _I, _P, _P]),
     "vs_integrate_depth_noalloc": (_I, [_P, _P, _P, ctypes.c_float, ctypes.c_float, ctypes.c_float, _P, _I, _I, _P,
                                         _P, _P, _P]),
     "vs_batch_create": (_I, [ctypes.POINTER(_P)]),
@@ -668,6 +670,20 @@ class Server:
 
     def clock(self):
         return self.lib.vs_server_clock()
+
+
+def warp_depth_to_color(depth_dev, w_d, h_d, K_d, T_rgb_wrt_d, K_rgb, w_rgb, h_rgb, out_dev, stream=None, mm_scale=None):
+    """depth (device pointer, float metres, or uint16 units when mm_scale is given) seen from the colour camera"""
+    kd = np.ascontiguousarray(K_d, np.float32)
+    kr = np.ascontiguousarray(K_rgb, np.float32)
+    t = np.ascontiguousarray(T_rgb_wrt_d, np.float32).reshape(16)
+    lib = load()
+    if mm_scale is None:
+        _check(lib.vs_warp_depth_to_color(_ptr(depth_dev), w_d, h_d, _ptr(kd), _ptr(t), _ptr(kr), w_rgb, h_rgb,
+                                          _ptr(out_dev), _ptr(stream)))
+    else:
+        _check(lib.vs_warp_depth_mm_to_color(_ptr(depth_dev), w_d, h_d, mm_scale, _ptr(kd), _ptr(t), _ptr(kr), w_rgb,
+                                             h_rgb, _ptr(out_dev), _ptr(stream)))
 
 
 def synth_config(width, height, **kw):
