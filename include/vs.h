@@ -167,6 +167,51 @@ int vs_set_color_volume(vs_session* s, const uint8_t* rgb_host);
 /* the colour image of the last frame's ray-cast at a level, planar */
 int vs_get_color_map(vs_session* s, int level, uint8_t* rgb_host);
 
+/* ---- scene rendering and valid-volume carving --------------------------------
+ * Render variants of LGKvRendererTSDF (z_yooji_cuda_tsdf_renderer.cu).  All
+ * write external device outputs only (the session's model maps are not
+ * touched) in the layout of vs_render_maps; normals stay in the global frame
+ * and the shaded image uses them with `light` as given.  Where nothing is
+ * hit: depth 0, vertex and normal -100, image 0. */
+
+/* rmis_Render_Maps_for_Scene with a vertex map (:1761-1814, kernel
+ * :1338-1446), the scanner's per-frame ray-cast for scene input
+ * (z_yooji_object_scanner.cpp:1318): level-0 size and intrinsics; every ray
+ * starts at the camera centre and ends 2 r_cube away, with no test against
+ * the cube's view cone (d_crtcs_Cast_Ray_on_TSDF_Cube_for_Scene, :908-1066);
+ * vertex in the camera frame; colour (optional, colour sessions) of the
+ * nearest voxel with weight > 0 (d_grvu, :155-229), 0 otherwise.  The
+ * reference writes the green channel into the red plane there, marked as
+ * temporary; the true red is written here. */
+int vs_render_maps_scene(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, float* map_depth_dev, float* map_vertex_dev,
+                         float* map_normals_dev, uint8_t* img_normals_dev, uint8_t* img_color_dev);
+/* rmis_Render_Maps_for_Scene without a vertex map (:1817-1862, kernel
+ * :1448-1548), the viewer's render (VCL_Volume_Scanner_View.cpp:1921): the
+ * scene ray-cast with the trilinear colour of vs_render_maps_color. */
+int vs_render_view_scene(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, float* map_depth_dev, float* map_normals_dev,
+                         uint8_t* img_normals_dev, uint8_t* img_color_dev);
+/* rmi_Render_Maps_for_ICP without a vertex map (:1703-1757, kernel
+ * :1211-1336): the object ray-cast of vs_render_maps at `level`, normals in
+ * the global frame, trilinear colour, and colour 255 in every channel where
+ * nothing is hit. */
+int vs_render_view(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                   const float* cam_cen, const float* light, int level, float* map_depth_dev,
+                   float* map_normals_dev, uint8_t* img_normals_dev, uint8_t* img_color_dev);
+
+/* LGKvVolumeIntegrator::uvv_Update_Valid_Volume
+ * (z_yooji_cuda_volume_integrator.cu:1035-1060, kernel :718-799): carve the
+ * volume with a valid-voxel mask (e.g. a visual hull), one byte per voxel
+ * (0 = outside), dim[0]*dim[1]*dim[2] bytes x fastest; a device pointer must
+ * be 8-byte aligned.  Each 8^3 sub-cube that the last integration activated
+ * (the reference's cube_valid flags) and that holds no valid voxel is reset
+ * to the empty state (TSDF 1, weight 0, colour 0) and loses its flag, so a
+ * second carving before the next integration leaves it alone.  Sub-cubes
+ * with at least one valid voxel are kept whole.  *carved (optional): the
+ * number of sub-cubes reset. */
+int vs_update_valid_volume(vs_session* s, const uint8_t* vol_valid, int is_host, uint32_t* carved);
+
 /* ---- depth -> colour camera registration ------------------------------------
  * z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates
  * (z_yooji_object_scanner.cpp:2429-2476): the depth map as seen from a second

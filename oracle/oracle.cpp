@@ -1074,16 +1074,23 @@ bool surface_normal(const Volume<T>& V, V3<T> p3d, V3<T>& nout) {
 // CUDA kernel stop after max_ray_iterations() steps and report no hit.
 inline int max_ray_iterations(float total_step_max) { return 4 * (int)total_step_max + 64; }
 
+// object mode: d_crtc_Cast_Ray_on_TSDF_Cube_NEW (z_yooji_cuda_tsdf_renderer.cu
+// :466-635), the ray segment through the cube's bounding sphere, rays outside
+// the cube's view cone rejected; scene mode: d_crtcs_Cast_Ray_on_TSDF_Cube_for
+// _Scene (:908-1066), from the camera centre to 2 r_cube, no cone test.  The
+// march itself is the same in both.
 template <class T>
 bool cast_ray(const Volume<T>& V, int lev, T px, T py, const T* T_cg, V3<T> cam, V3<T> ncc,
-              T dist_cc, T theta_max, V3<T>& p3d) {
+              T dist_cc, T theta_max, V3<T>& p3d, bool scene = false) {
   const Cfg<T>& g = V.g;
   enum { COARSE, FINE, BEHIND };
-  T dmin = dist_cc - g.r_cube, dmax = dist_cc + g.r_cube;
+  T dmin = scene ? T(0) : dist_cc - g.r_cube, dmax = scene ? T(2) * g.r_cube : dist_cc + g.r_cube;
   V3<T> pe = transform(back_project(px, py, g.K[lev], dmax), T_cg);
   V3<T> rd = normalised(pe - cam);
-  T theta = std::acos(dot(rd, ncc));
-  if (theta > theta_max) return false;
+  if (!scene) {
+    T theta = std::acos(dot(rd, ncc));
+    if (theta > theta_max) return false;
+  }
   V3<T> ps = cam + dmin * rd;
   T step_scale = T(0.9f) * g.mu * g.vox_inv;
   T step = step_scale, coarse = step_scale;
@@ -1173,9 +1180,38 @@ void trilinear_color(const Volume<T>& V, V3<T> pg, uint8_t out[3]) {
   }
 }
 
+// d_grvu_Get_RGB_Value_Uninterpolated (z_yooji_cuda_tsdf_renderer.cu:155-229):
+// the colour of the nearest voxel (ROUNDF) when it is in range with weight > 0,
+// else 0.  The reference's Vector3u overload reads the green plane for red
+// (:178), and the scene kernel writes green into the red plane (:1432-1434,
+// marked there as temporary); the true red is returned here.
+template <class T>
+void nearest_color(const Volume<T>& V, V3<T> pg, uint8_t out[3]) {
+  out[0] = out[1] = out[2] = 0;
+  if (V.col.empty()) return;
+  const Cfg<T>& g = V.g;
+  V3<T> pv;
+  pos_in_voxel(pg, g.origin, g.dim, g.vox_inv, pv);
+  if (std::isnan(pv.x) || std::isnan(pv.y) || std::isnan(pv.z)) return;
+  const int x = roundf_ref(pv.x), y = roundf_ref(pv.y), z = roundf_ref(pv.z);
+  if (x < 0 || x >= g.dim[0] || y < 0 || y >= g.dim[1] || z < 0 || z >= g.dim[2]) return;
+  const size_t n3 = (size_t)g.dim[0] * g.dim[1] * g.dim[2];
+  const size_t i = ((size_t)z * g.dim[1] + y) * g.dim[0] + x;
+  if (V.w[i] == 0) return;
+  for (int k = 0; k < 3; k++) out[k] = V.col[i + k * n3];
+}
+
+// render variants (bits of `mode`), as the CUDA library's
+enum { kRayScene = 1, kRayGlobalNormals = 2, kRayNearestColor = 4, kRayWhiteBackground = 8 };
+
+// mode 0: g_rmi_Render_Maps_for_ICP (z_yooji_cuda_tsdf_renderer.cu:1070-1209);
+// kRayScene | kRayGlobalNormals | kRayNearestColor: g_rmis with a vertex map
+// (:1338-1446); kRayScene | kRayGlobalNormals: g_rmis without one
+// (:1448-1548); kRayGlobalNormals | kRayWhiteBackground: g_rmi without one
+// (:1211-1336).  vtx may be NULL.
 template <class T>
 void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> cam, V3<T> light,
-             T* depth, T* vtx, T* nrm, uint8_t* img, uint8_t* rgb = nullptr) {
+             T* depth, T* vtx, T* nrm, uint8_t* img, uint8_t* rgb = nullptr, int mode = 0) {
   const Cfg<T>& g = V.g;
   const int w = g.W[lev], h = g.H[lev];
   V3<T> cc = v3(g.center[0], g.center[1], g.center[2]);
@@ -1188,14 +1224,16 @@ void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> ca
     for (int tx = 0; tx < w; tx++) {
       size_t t = (size_t)ty * w + tx;
       V3<T> pg, sn;
-      bool valid = cast_ray(V, lev, (T)tx, (T)ty, T_cg, cam, ncc, dist_cc, theta_max, pg);
+      bool valid = cast_ray(V, lev, (T)tx, (T)ty, T_cg, cam, ncc, dist_cc, theta_max, pg, (mode & kRayScene) != 0);
       if (valid && surface_normal(V, pg, sn)) {
         V3<T> pc = transform(pg, T_gc);
         depth[t] = pc.z;
-        vtx[3 * t] = pc.x;
-        vtx[3 * t + 1] = pc.y;
-        vtx[3 * t + 2] = pc.z;
-        V3<T> sc = rotate(sn, T_gc);
+        if (vtx) {
+          vtx[3 * t] = pc.x;
+          vtx[3 * t + 1] = pc.y;
+          vtx[3 * t + 2] = pc.z;
+        }
+        V3<T> sc = (mode & kRayGlobalNormals) ? sn : rotate(sn, T_gc);
         nrm[3 * t] = sc.x;
         nrm[3 * t + 1] = sc.y;
         nrm[3 * t + 2] = sc.z;
@@ -1205,16 +1243,19 @@ void raycast(const Volume<T>& V, int lev, const T* T_gc, const T* T_cg, V3<T> ca
         img[t] = (uint8_t)s;
         if (rgb) {
           uint8_t c[3];
-          trilinear_color(V, pg, c);
+          if (mode & kRayNearestColor)
+            nearest_color(V, pg, c);
+          else
+            trilinear_color(V, pg, c);
           for (int k = 0; k < 3; k++) rgb[t + k * (size_t)w * h] = c[k];
         }
       } else {
         depth[t] = 0;
-        vtx[3 * t] = vtx[3 * t + 1] = vtx[3 * t + 2] = T(-100);
+        if (vtx) vtx[3 * t] = vtx[3 * t + 1] = vtx[3 * t + 2] = T(-100);
         nrm[3 * t] = nrm[3 * t + 1] = nrm[3 * t + 2] = T(-100);
         img[t] = 0;
         if (rgb)
-          for (int k = 0; k < 3; k++) rgb[t + k * (size_t)w * h] = 0;
+          for (int k = 0; k < 3; k++) rgb[t + k * (size_t)w * h] = (mode & kRayWhiteBackground) ? 255 : 0;
       }
     }
 }
@@ -1537,6 +1578,46 @@ void or_warp_depth(const float* depth, int wd, int hd, const float* Kd, const fl
       float& cur = out[(size_t)ty * wr + tx];
       if (cur > td || cur <= 0.0f) cur = td;
     }
+}
+void or_render_variant(const or_volume* v, int level, int mode, const float* T_gc, const float* T_cg,
+                       const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,
+                       uint8_t* img, uint8_t* rgb) {
+  raycast<float>(v->v, level, T_gc, T_cg, v3(cam_cen[0], cam_cen[1], cam_cen[2]),
+                 v3(light[0], light[1], light[2]), depth, vtx3, nrm3, img, rgb, mode);
+}
+// g_uvv_Update_Valid_Volume (z_yooji_cuda_volume_integrator.cu:718-799): each
+// sub-cube flagged by the last integration (cube_valid) with no valid voxel is
+// reset (TSDF 1, weight 0, colour 0) and unflagged; returns the number reset
+uint32_t or_update_valid_volume(or_volume* ov, const uint8_t* valid) {
+  Volume<float>& V = ov->v;
+  const Cfg<float>& g = V.g;
+  const int X = g.dim[0], Y = g.dim[1], Z = g.dim[2];
+  const size_t n3 = (size_t)X * Y * Z;
+  uint32_t carved = 0;
+  for (int zs = 0; zs < V.nsc[2]; zs++)
+    for (int ys = 0; ys < V.nsc[1]; ys++)
+      for (int xs = 0; xs < V.nsc[0]; xs++) {
+        uint8_t& f = V.flags[((size_t)zs * V.nsc[1] + ys) * V.nsc[0] + xs];
+        if (!f) continue;
+        int cnt = 0;
+        for (int z = zs * 8; z < zs * 8 + 8 && z < Z; z++)
+          for (int y = ys * 8; y < ys * 8 + 8 && y < Y; y++)
+            for (int x = xs * 8; x < xs * 8 + 8 && x < X; x++)
+              if (valid[((size_t)z * Y + y) * X + x]) cnt++;
+        if (cnt > 0) continue;
+        f = 0;
+        carved++;
+        for (int z = zs * 8; z < zs * 8 + 8 && z < Z; z++)
+          for (int y = ys * 8; y < ys * 8 + 8 && y < Y; y++)
+            for (int x = xs * 8; x < xs * 8 + 8 && x < X; x++) {
+              const size_t i = ((size_t)z * Y + y) * X + x;
+              V.tsdf[i] = store_tsdf<float>(1.0f, g.tsdf_store);
+              V.w[i] = 0;
+              if (!V.col.empty())
+                for (int k = 0; k < 3; k++) V.col[i + k * n3] = 0;
+            }
+      }
+  return carved;
 }
 uint64_t or_extract_mesh(const or_volume* v, float* xyz, uint8_t* rgb, uint64_t capacity) {
   return extract_mesh<float>(v->v, xyz, rgb, capacity);

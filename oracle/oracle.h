@@ -95,6 +95,13 @@ void or_volume_get(const or_volume* v, float* tsdf, uint16_t* w);
 void or_volume_set(or_volume* v, const float* tsdf, const uint16_t* w);
 /* flags of the last integrate call, one byte per 8^3 sub-cube */
 void or_volume_flags(const or_volume* v, uint8_t* flags);
+/* render variants: mode bits 1 scene ray-cast, 2 global normals, 4 nearest-voxel
+ * colour, 8 colour 255 where nothing is hit; vtx3 / rgb may be NULL */
+void or_render_variant(const or_volume* v, int level, int mode, const float* T_gc, const float* T_cg,
+                       const float* cam_cen, const float* light, float* depth, float* vtx3, float* nrm3,
+                       uint8_t* img, uint8_t* rgb);
+/* valid-volume carving over the last integration's sub-cube flags */
+uint32_t or_update_valid_volume(or_volume* v, const uint8_t* valid);
 /* reference integration: sub-cube activation then TSDF update */
 void or_integrate(or_volume* v, const float* depth, const float* T_gc,
                   const float* T_cg);

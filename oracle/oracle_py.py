@@ -17,6 +17,8 @@ _ref = None
 ORACLE_REDUCE_FROM_VS = {0: 1, 1: 2, 2: 3}
 # oracle tsdf_store: 0 fp32, 1 int16, 2 fp16 ; vs tsdf_type: 0 int16, 1 fp16, 2 fp32
 ORACLE_STORE_FROM_VS = {0: 1, 1: 2, 2: 0}
+# render variant bits (or_render_variant)
+RAY_SCENE, RAY_GLOBAL_NORMALS, RAY_NEAREST_COLOR, RAY_WHITE_BACKGROUND = 1, 2, 4, 8
 
 
 class OrConfig(ctypes.Structure):
@@ -78,6 +80,8 @@ def load():
             "or_volume_set_color": (None, [P, P]),
             "or_raycast_color": (None, [P, I, P, P, P, P, P, P, P, P, P]),
             "or_extract_mesh": (ctypes.c_uint64, [P, P, P, ctypes.c_uint64]),
+            "or_render_variant": (None, [P, I, I, P, P, P, P, P, P, P, P, P]),
+            "or_update_valid_volume": (ctypes.c_uint32, [P, P]),
             "or_warp_depth": (None, [P, I, I, P, P, P, I, I, P]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
@@ -345,6 +349,28 @@ class Volume:
         self.lib.or_raycast_color(self.h, level, _p(a), _p(b), _p(c), _p(l), _p(dep), _p(v), _p(n), _p(img),
                                   _p(rgb))
         return dep, v, n, img, rgb
+
+    def render_variant(self, mode, level, T_gc, T_cg, cam, light=(0.0, 0.0, -1.0), vertex=True, color=False):
+        """mode: RAY_* bits; returns depth, vertex (or None), normals, image, colour (or None)"""
+        w, h = level_sizes(self.cfg)[level]
+        a = np.ascontiguousarray(T_gc, np.float32).reshape(16)
+        b = np.ascontiguousarray(T_cg, np.float32).reshape(16)
+        c = np.ascontiguousarray(cam, np.float32)
+        l = np.ascontiguousarray(light, np.float32)
+        dep = np.empty((h, w), np.float32)
+        v = np.empty((h, w, 3), np.float32) if vertex else None
+        n = np.empty((h, w, 3), np.float32)
+        img = np.empty((h, w), np.uint8)
+        rgb = np.empty((3, h, w), np.uint8) if color else None
+        self.lib.or_render_variant(self.h, level, mode, _p(a), _p(b), _p(c), _p(l), _p(dep), _p(v) if vertex else None,
+                                   _p(n), _p(img), _p(rgb) if color else None)
+        return dep, v, n, img, rgb
+
+    def update_valid_volume(self, valid):
+        """valid: one byte per voxel, x fastest; returns the sub-cubes reset"""
+        m = np.ascontiguousarray(valid, np.uint8).reshape(-1)
+        assert m.size == self.n
+        return int(self.lib.or_update_valid_volume(self.h, _p(m)))
 
     def raycast(self, level, T_gc, T_cg, cam, light=(0.0, 0.0, -1.0)):
         w, h = level_sizes(self.cfg)[level]

@@ -66,12 +66,23 @@ __global__ void k_session_tables(SessionDev* s) {
   }
 }
 
-// frame counters of every slot
-__global__ void k_integrate_prepare(const BatchTable* __restrict__ bt) {
+// frame counters of every slot, and the activation stamp.  A brick's flag
+// holds the stamp of the last integration that activated it, so no pass
+// clears flags: the flagged set of the last integration is {b : flag[b] ==
+// stamp != 0}, the reference's per-sub-cube bytes (cube_valid) after its
+// reset and marking (z_yooji_cuda_volume_integrator.cu:1006-1016), which
+// g_uvv_Update_Valid_Volume visits later.  A session whose tracking failed
+// (gate) does not integrate and keeps its stamp and flags.
+__global__ void k_integrate_prepare(const BatchTable* __restrict__ bt, int gate) {
   const int i = threadIdx.x;
   if (i < bt->n) {
-    bt->s[i]->brick_count[0] = 0u;
-    bt->s[i]->brick_count[1] = 0u;
+    const SessionDev* s = bt->s[i];
+    s->brick_count[0] = 0u;
+    s->brick_count[1] = 0u;
+    if (!(gate && s->pose->failed)) {
+      const uint32_t stamp = s->brick_count[2] + 1u;
+      s->brick_count[2] = stamp ? stamp : 1u;
+    }
   }
 }
 
@@ -100,6 +111,7 @@ __global__ void __launch_bounds__(256) k_activate(const BatchTable* __restrict__
     F3 pe = transform(back_project((float)x, (float)y, K, 100.0f), T);
     F3 dv = normalised(sub(pe, p));
     const int nb0 = s->nb[0], nb1 = s->nb[1], nb2 = s->nb[2];
+    const uint32_t stamp = s->brick_count[2];
     int prev = -1;
     for (int m = -4; m <= 1; m++) {
       F3 tp = add(p, scale(((float)m) * s->mu, dv));
@@ -111,7 +123,7 @@ __global__ void __launch_bounds__(256) k_activate(const BatchTable* __restrict__
       if (b == prev) continue;
       prev = b;
       uint32_t* f = s->brick_flag + b;
-      if (*((volatile uint32_t*)f) == 0u && atomicExch(f, 1u) == 0u) {
+      if (*((volatile uint32_t*)f) != stamp && atomicExch(f, stamp) != stamp) {
         uint32_t pos = atomicAdd(s->brick_count, 1u);
         s->brick_list[pos] = (uint32_t)b;
       }
@@ -126,7 +138,6 @@ struct IntParams {
   const float* lut_ray;
   const float* lam_map;
   const uint32_t* list;
-  uint32_t* flag;
   uint32_t* counters;
   uint32_t* occ;
   uint32_t* occ1;
@@ -149,7 +160,6 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.lut_ray = s->lut_ray;
   q.lam_map = s->lam_map;
   q.list = s->brick_list;
-  q.flag = s->brick_flag;
   q.counters = s->brick_count;
   q.occ = s->occ;
   q.occ1 = s->occ1;
@@ -411,7 +421,6 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
     if (lane == 0) {
-      q.flag[b] = 0u;
       if (nupd) {
         atomicAdd(q.counters + 1, (uint32_t)nupd);
         // weights never decrease, so a brick that got an update, and the
@@ -587,7 +596,7 @@ void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) 
 void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc, const float* Tcg,
                       bool gate, cudaStream_t st, bool color) {
   const int c = color ? 1 : 0;
-  k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt);
+  k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt, gate ? 1 : 0);
   k_activate<<<sm_count() * 8, dim3(32, 8), 0, st>>>(bt, depth, Tcg, gate ? 1 : 0);
   // persistent grid: every block resident at once
   switch (tsdf_type) {
@@ -648,6 +657,49 @@ void launch_volume_slab(const SessionDev& h, bool do_export, int z0, int nz, flo
       break;
   }
 }
+// g_uvv_Update_Valid_Volume (z_yooji_cuda_volume_integrator.cu:718-799, host
+// :1035-1060): every sub-cube flagged by the last integration whose voxels
+// are all invalid in `valid` (one byte per voxel, x fastest, 0 = invalid) is
+// reset to the empty state (TSDF 1, weight 0, colour 0) and unflagged;
+// sub-cubes with a valid voxel, and unflagged ones, are left as they are.
+// One warp per brick: a lane tests rows 2 lane and 2 lane + 1 (8 bytes
+// each, aligned: dim[0] is a multiple of 8 and `valid` 8-byte aligned).  The
+// brick's occupancy bit is cleared (it holds no weight any more); the coarse
+// cells around it stay set, which only costs the ray-caster a skip.
+template <class S>
+__global__ void k_carve(const SessionDev* __restrict__ s, const uint8_t* __restrict__ valid, unsigned* carved) {
+  typename S::word* vol = reinterpret_cast<typename S::word*>(s->vol);
+  const int nb0 = s->nb[0], nb1 = s->nb[1];
+  const size_t nbr = (size_t)nb0 * nb1 * s->nb[2];
+  const size_t X = (size_t)s->dim[0], XY = X * (size_t)s->dim[1];
+  const uint32_t stamp = s->brick_count[2];
+  const int lane = threadIdx.x & 31;
+  const size_t gw = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarp = ((size_t)gridDim.x * blockDim.x) >> 5;
+  for (size_t b = gw; b < nbr; b += nwarp) {
+    const uint32_t f = s->brick_flag[b];
+    if (f == 0u || f != stamp) continue;  // the same for the whole warp
+    const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / ((size_t)nb0 * nb1));
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 2; k++) {
+      const int r = 2 * lane + k;
+      const size_t o = (size_t)(bz * 8 + (r >> 3)) * XY + (size_t)(by * 8 + (r & 7)) * X + (size_t)bx * 8;
+      const uint2 v = __ldg(reinterpret_cast<const uint2*>(valid + o));
+      any |= (v.x | v.y) != 0u;
+    }
+    if (__any_sync(0xffffffffu, any)) continue;
+    const typename S::word e = S::initial();
+    for (int k = lane; k < kBrickVox; k += 32) vol[b * kBrickVox + k] = e;
+    if (s->col)
+      for (int k = lane; k < kBrickVox; k += 32) s->col[b * kBrickVox + k] = 0u;
+    if (lane == 0) {
+      s->brick_flag[b] = 0u;
+      atomicAnd(s->occ + (b >> 5), ~(1u << (b & 31)));
+      atomicAdd(carved, 1u);
+    }
+  }
+}
 
 size_t occupancy_words(const SessionDev& h, int level) {
   if (level == 0) return (((size_t)h.nb[0] * h.nb[1] * h.nb[2]) + 31) / 32;
@@ -673,6 +725,21 @@ void launch_occupancy_rebuild(const SessionDev& h, const SessionDev* d, cudaStre
       break;
     default:
       k_occupancy<StoreI16><<<blocks, 256, 0, st>>>(d);
+      break;
+  }
+}
+
+void launch_carve(const SessionDev& h, const SessionDev* d, const uint8_t* valid, unsigned* carved, cudaStream_t st) {
+  const int blocks = sm_count() * 8;
+  switch (h.tsdf_type) {
+    case VS_TSDF_FP16:
+      k_carve<StoreF16><<<blocks, 256, 0, st>>>(d, valid, carved);
+      break;
+    case VS_TSDF_FP32:
+      k_carve<StoreF32><<<blocks, 256, 0, st>>>(d, valid, carved);
+      break;
+    default:
+      k_carve<StoreI16><<<blocks, 256, 0, st>>>(d, valid, carved);
       break;
   }
 }

@@ -43,6 +43,7 @@ struct RayArgs {
   float* out_nrm3;
   uint8_t* out_img;
   uint8_t* out_rgb;     // planar colour image (NULL: none)
+  int mode;             // kRay* bits of the external render variants (0: the ICP maps)
 };
 
 // Volume reads.  A brick whose occupancy bit is clear has weight 0 in every
@@ -253,13 +254,15 @@ __device__ bool surface_normal(const Vol<S>& V, const SessionDev& s, F3 p3d, F3&
 
 template <class S>
 __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, float px, float py,
-                         const float* Tcg, F3 cam, F3 ncc, float dist_cc, float theta_max, F3& p3d) {
+                         const float* Tcg, F3 cam, float dmin, float dmax, bool cone, F3 ncc, float theta_max,
+                         F3& p3d) {
   enum { COARSE, FINE, BEHIND };
-  const float dmin = dist_cc - s.r_cube, dmax = dist_cc + s.r_cube;
   F3 pe = transform(back_project(px, py, K, dmax), Tcg);
   F3 rd = normalised(sub(pe, cam));
-  float theta = acosf(dot(rd, ncc));
-  if (theta > theta_max) return false;
+  if (cone) {
+    float theta = acosf(dot(rd, ncc));
+    if (theta > theta_max) return false;
+  }
   F3 ps = add(cam, scale(dmin, rd));
   const float step_scale = 0.9f * s.mu * s.vox_inv;
   const float total_max = 2.0f * s.r_cube * s.vox_inv;
@@ -412,7 +415,7 @@ __device__ inline Vol<S> volume_of(const SessionDev& s) {
 
 // phase 1: march every ray to its surface point (global coordinates; w = 1
 // hit, 0 none) in the session's hit buffer
-template <class S>
+template <class S, bool SCENE>
 __global__ void __launch_bounds__(kRayThreads, VS_RAY_MIN_BLOCKS) k_ray_march(RayArgs a) {
   for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
     const Vol<S> V = volume_of<S>(s);
@@ -432,7 +435,12 @@ __global__ void __launch_bounds__(kRayThreads, VS_RAY_MIN_BLOCKS) k_ray_march(Ra
     const float dist_cc = length(vcc);
     const float theta_max = asinf(s.r_cube / dist_cc);
     F3 pg;
-    const bool hit = cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, ncc, dist_cc, theta_max, pg);
+    // object mode (d_crtc_NEW, :466-635): the segment of the ray through the
+    // cube's bounding sphere inside its view cone; scene mode (d_crtcs,
+    // :908-1066): from the camera centre to 2 r_cube, no cone
+    const float dmin = SCENE ? 0.0f : dist_cc - s.r_cube;
+    const float dmax = SCENE ? 2.0f * s.r_cube : dist_cc + s.r_cube;
+    const bool hit = cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, dmin, dmax, !SCENE, ncc, theta_max, pg);
     s.ray_hit[hit_offset(s, l) + (size_t)y * s.lv[l].W + x] =
         hit ? make_float4(pg.x, pg.y, pg.z, 1.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   });
@@ -481,6 +489,22 @@ __device__ uint32_t trilinear_color(const Vol<S>& V, const SessionDev& s, F3 pg)
   return pack_rgb(out[0], out[1], out[2]);
 }
 
+// d_grvu_Get_RGB_Value_Uninterpolated (z_yooji_cuda_tsdf_renderer.cu:155-229)
+// for the scene maps: the colour of the nearest voxel (ROUNDF) if it is in
+// range with weight > 0, else 0.  (The reference's scene image writes the green
+// channel into the red plane, marked there as temporary; the true colour is
+// written here.)
+template <class S>
+__device__ uint32_t nearest_color(const Vol<S>& V, const SessionDev& s, F3 pg) {
+  F3 v;
+  pos_in_voxel(pg, s, v);
+  if (isnan(v.x) || isnan(v.y) || isnan(v.z)) return 0u;
+  const int x = roundf_ref(v.x), y = roundf_ref(v.y), z = roundf_ref(v.z);
+  float t;
+  if (!V.at_any(x, y, z, t)) return 0u;
+  return __ldg(s.col + brick_word_index(x, y, z, V.nb));
+}
+
 // phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
 // normal, shading, colour, into the model maps or the external outputs
 template <class S, bool COLOR>
@@ -498,22 +522,25 @@ __global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(
     uint32_t rgb = 0u;
     F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
     if (valid) {
-      if (COLOR && s.col) rgb = trilinear_color(V, s, pg);
+      if (COLOR && s.col) rgb = (a.mode & kRayNearestColor) ? nearest_color(V, s, pg) : trilinear_color(V, s, pg);
       const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
       float Tgc[12];
 #pragma unroll
       for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k];
       pc = transform(pg, Tgc);
       dep = pc.z;
-      sc = rotate(sn, Tgc);
+      sc = (a.mode & kRayGlobalNormals) ? sn : rotate(sn, Tgc);
       float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
       img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
     }
     if (ext) {
+      if (!valid && (a.mode & kRayWhiteBackground)) rgb = 0x00ffffffu;
       a.out_depth[idx] = dep;
-      a.out_vtx3[3 * idx] = pc.x;
-      a.out_vtx3[3 * idx + 1] = pc.y;
-      a.out_vtx3[3 * idx + 2] = pc.z;
+      if (a.out_vtx3) {
+        a.out_vtx3[3 * idx] = pc.x;
+        a.out_vtx3[3 * idx + 1] = pc.y;
+        a.out_vtx3[3 * idx + 2] = pc.z;
+      }
       a.out_nrm3[3 * idx] = sc.x;
       a.out_nrm3[3 * idx + 1] = sc.y;
       a.out_nrm3[3 * idx + 2] = sc.z;
@@ -570,7 +597,7 @@ int max_per_sm(K kernel) {
 
 template <class S>
 int ray_max_per_sm(bool shade) {
-  static const int m = max_per_sm(k_ray_march<S>);
+  static const int m = max_per_sm(k_ray_march<S, false>);
   static const int h = max_per_sm(k_ray_shade<S, false>);
   return shade ? h : m;
 }
@@ -580,7 +607,10 @@ int grid_of(int want, int most) { return sm_count() * ((want > 0 && want < most)
 template <class S>
 void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, bool color, cudaStream_t st) {
   RayArgs a = a0;
-  k_ray_march<S><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
+  if (a.mode & kRayScene)
+    k_ray_march<S, true><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
+  else
+    k_ray_march<S, false><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
   a.work = a0.work + 4;
   static const int most_color = max_per_sm(k_ray_shade<S, true>);
   if (color)
@@ -592,7 +622,7 @@ void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, bool color, 
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate, float* out_depth, float* out_vtx3,
                     float* out_nrm3, uint8_t* out_img, cudaStream_t st, const LaunchShape& shape, uint8_t* out_rgb,
-                    bool color) {
+                    bool color, int mode) {
   RayArgs a;
   a.bt = bt;
   a.work = const_cast<unsigned*>(bt->work);  // [0..1] march, [4..5] shade
@@ -609,6 +639,7 @@ void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float*
   a.out_nrm3 = out_nrm3;
   a.out_img = out_img;
   a.out_rgb = out_rgb;
+  a.mode = mode;
   switch (tsdf_type) {
     case VS_TSDF_FP16:
       launch_ray_phases<StoreF16>(a, shape, color, st);

@@ -157,7 +157,7 @@ int reset_state(vs_session* s) {
   VS_CU(cudaGetLastError());
   VS_CU(cudaMemsetAsync(s->h.brick_flag, 0, sizeof(uint32_t) * (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2],
                         s->stream));
-  VS_CU(cudaMemsetAsync(s->h.brick_count, 0, sizeof(uint32_t), s->stream));
+  VS_CU(cudaMemsetAsync(s->h.brick_count, 0, 4 * sizeof(uint32_t), s->stream));
   launch_occupancy_clear(s->h, s->stream);
   VS_CU(cudaGetLastError());
   VS_CU(cudaMemsetAsync(s->h.icp_counter, 0, sizeof(unsigned), s->stream));
@@ -505,6 +505,80 @@ int vs_render_maps_color(vs_session* s, int ww, int hh, const float* T_gc_dev, c
                  false, depth_dev, vtx_dev, nrm_dev, img_dev, s->stream, LaunchShape(), rgb_dev, true);
   VS_CU(cudaGetLastError());
   VS_CU(cudaStreamSynchronize(s->stream));
+  return VS_OK;
+}
+
+// the ray-cast variants that write external outputs only
+static int render_variant(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                          const float* cam_cen, const float* light, int level, float* depth_dev, float* vtx_dev,
+                          float* nrm_dev, uint8_t* img_dev, uint8_t* rgb_dev, int mode) {
+  if (!s || !T_gc_dev || !T_cg_dev || !cam_cen || !light || !depth_dev || !nrm_dev || !img_dev)
+    return fail(VS_ERR_ARG, "null argument");
+  if (rgb_dev && !s->h.col) return fail(VS_ERR_STATE, "session has no colour volume (cfg.color = 0)");
+  if (level < 0 || level >= s->h.levels) return fail(VS_ERR_ARG, "bad level");
+  if (ww != s->h.lv[level].W || hh != s->h.lv[level].H) return fail(VS_ERR_ARG, "size differs from the level");
+  VS_CU(cudaMemcpyAsync(s->dev_small, cam_cen, 3 * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  launch_raycast(s->tab, s->h.tsdf_type, level, T_gc_dev, T_cg_dev, s->dev_small, light[0], light[1], light[2],
+                 false, depth_dev, vtx_dev, nrm_dev, img_dev, s->stream, LaunchShape(), rgb_dev, rgb_dev != nullptr,
+                 mode);
+  VS_CU(cudaGetLastError());
+  VS_CU(cudaStreamSynchronize(s->stream));
+  return VS_OK;
+}
+
+int vs_render_maps_scene(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, float* depth_dev, float* vtx_dev, float* nrm_dev,
+                         uint8_t* img_dev, uint8_t* rgb_dev) {
+  if (!vtx_dev) return fail(VS_ERR_ARG, "null argument");
+  return render_variant(s, ww, hh, T_gc_dev, T_cg_dev, cam_cen, light, 0, depth_dev, vtx_dev, nrm_dev, img_dev,
+                        rgb_dev, kRayScene | kRayGlobalNormals | kRayNearestColor);
+}
+
+int vs_render_view_scene(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                         const float* cam_cen, const float* light, float* depth_dev, float* nrm_dev, uint8_t* img_dev,
+                         uint8_t* rgb_dev) {
+  return render_variant(s, ww, hh, T_gc_dev, T_cg_dev, cam_cen, light, 0, depth_dev, nullptr, nrm_dev, img_dev,
+                        rgb_dev, kRayScene | kRayGlobalNormals);
+}
+
+int vs_render_view(vs_session* s, int ww, int hh, const float* T_gc_dev, const float* T_cg_dev,
+                   const float* cam_cen, const float* light, int level, float* depth_dev, float* nrm_dev,
+                   uint8_t* img_dev, uint8_t* rgb_dev) {
+  return render_variant(s, ww, hh, T_gc_dev, T_cg_dev, cam_cen, light, level, depth_dev, nullptr, nrm_dev, img_dev,
+                        rgb_dev, kRayGlobalNormals | kRayWhiteBackground);
+}
+
+int vs_update_valid_volume(vs_session* s, const uint8_t* vol_valid, int is_host, uint32_t* carved) {
+  if (!s || !vol_valid) return fail(VS_ERR_ARG, "null argument");
+  const size_t n = (size_t)s->h.dim[0] * s->h.dim[1] * s->h.dim[2];
+  const uint8_t* v = vol_valid;
+  uint8_t* tmp = nullptr;
+  if (is_host) {
+    VS_CU(cudaMallocAsync(reinterpret_cast<void**>(&tmp), n, s->stream));
+    cudaError_t e = cudaMemcpyAsync(tmp, vol_valid, n, cudaMemcpyHostToDevice, s->stream);
+    if (e != cudaSuccess) {
+      cudaFreeAsync(tmp, s->stream);
+      return cuda_fail(e, "cudaMemcpyAsync");
+    }
+    v = tmp;
+  } else if (reinterpret_cast<uintptr_t>(vol_valid) % 8) {
+    return fail(VS_ERR_ARG, "vol_valid must be 8-byte aligned");
+  }
+  unsigned* d_count = reinterpret_cast<unsigned*>(s->dev_small + 4);
+  cudaError_t e = cudaMemsetAsync(d_count, 0, sizeof(unsigned), s->stream);
+  if (e == cudaSuccess) {
+    launch_carve(s->h, s->d, v, d_count, s->stream);
+    e = cudaGetLastError();
+  }
+  unsigned c = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&c, d_count, sizeof(unsigned), cudaMemcpyDeviceToHost, s->stream);
+  if (tmp) {
+    const cudaError_t e2 = cudaFreeAsync(tmp, s->stream);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "vs_update_valid_volume");
+  if (carved) *carved = c;
   return VS_OK;
 }
 

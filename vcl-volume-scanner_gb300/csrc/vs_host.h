@@ -19,7 +19,7 @@ struct vs_session {
   cudaGraphExec_t exec = nullptr;
   std::vector<void*> allocs;
   float* stage_f = nullptr;      // level-0 float staging (bfd input)
-  float* dev_small = nullptr;    // 16 floats of scratch (camera centre)
+  float* dev_small = nullptr;    // 16 floats of scratch: [0..2] camera centre, [4] carve counter
   vs::Pose* host_pose = nullptr;     // pinned
   int device = 0;
   bool timing = false;           // stage events recorded inside the graph

@@ -78,9 +78,9 @@ struct SessionDev {
   uint8_t* m_img[kMaxLevels];
   // volume
   void* vol;                     // bricks, 512 words each
-  uint32_t* brick_flag;          // per brick: 1 while listed this frame
+  uint32_t* brick_flag;          // per brick: stamp of the last integration that listed it (0: never / carved)
   uint32_t* brick_list;          // active bricks of this frame
-  uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame)
+  uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame), [2] activation stamp
   uint32_t* occ;                 // 1 bit per brick: some voxel has weight > 0 (NULL: not kept)
   uint32_t* occ1;                // 1 bit per 4^3 bricks (32^3 voxels): some brick occupied
   uint32_t* occ2;                // 1 bit per 16^3 bricks (128^3 voxels)
@@ -298,10 +298,19 @@ void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, c
 void launch_raycast(const BatchTable* bt, int tsdf_type, int level, const float* Tgc, const float* Tcg,
                     const float* center, float lx, float ly, float lz, bool gate_on_tracking, float* out_depth,
                     float* out_vtx3, float* out_nrm3, uint8_t* out_img, cudaStream_t st,
-                    const LaunchShape& shape = LaunchShape(), uint8_t* out_rgb = nullptr, bool color = false);
+                    const LaunchShape& shape = LaunchShape(), uint8_t* out_rgb = nullptr, bool color = false,
+                    int mode = 0);
+// render variants (launch_raycast mode bits, external outputs only)
+constexpr int kRayScene = 1;           // d_crtcs: camera centre to 2 r_cube, no cone test
+constexpr int kRayGlobalNormals = 2;   // normals left in the global frame
+constexpr int kRayNearestColor = 4;    // d_grvu nearest-voxel colour instead of d_grvi
+constexpr int kRayWhiteBackground = 8; // colour 255 where nothing is hit
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st);
 // planar colour frame -> one word per pixel (rgb: a device frame, or NULL for the session's own)
 void launch_pack_color(const SessionDev& h, const uint8_t* rgb, cudaStream_t st);
+// g_uvv_Update_Valid_Volume: valid = one byte per voxel, x fastest, 8-byte
+// aligned; *carved (device) counts the sub-cubes reset
+void launch_carve(const SessionDev& h, const SessionDev* d, const uint8_t* valid, unsigned* carved, cudaStream_t st);
 // colour volume <-> reference layout (three planes of x-fastest bytes)
 void launch_color_volume(const SessionDev& h, bool do_export, uint8_t* planes, cudaStream_t st);
 void launch_color_map_export(const SessionDev& h, int level, uint8_t* planes, cudaStream_t st);

@@ -13,11 +13,14 @@
 //   uint32   index[n]      ascending
 //   words    n * 512 TSDF words (4 bytes, 8 for the FP32 storage)
 //   uint32   n * 512 colour words (sessions with colour only)
+//   uint64   m             sub-cubes the last integration flagged (optional)
+//   uint32   flagged[m]    ascending
 // Only sub-cubes whose occupancy bit is set carry data; every other voxel is in
 // its initial state.  Loading creates a session with the saved configuration,
 // scatters the sub-cubes, rebuilds the occupancy levels, restores the pose and
-// ray-casts the model maps from it, which is what the saved session's next
-// frame would read.
+// the flagged set (what a valid-volume carving visits), and ray-casts the
+// model maps from the pose, which is what the saved session's next frame would
+// read.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -58,6 +61,23 @@ int occupied_bricks(vs_session* s, std::vector<uint32_t>& out) {
   return VS_OK;
 }
 
+// ascending indices of the sub-cubes flagged by the last integration
+// (flag == activation stamp != 0)
+int flagged_bricks(vs_session* s, std::vector<uint32_t>& out) {
+  const size_t nbr = (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2];
+  std::vector<uint32_t> flags(nbr);
+  uint32_t cnt[4];
+  cudaError_t e = cudaStreamSynchronize(s->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(flags.data(), s->h.brick_flag, nbr * 4, cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(cnt, s->h.brick_count, sizeof(cnt), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail_code(e, "sub-cube flags read");
+  out.clear();
+  if (cnt[2] == 0u) return VS_OK;
+  for (size_t b = 0; b < nbr; b++)
+    if (flags[b] == cnt[2]) out.push_back((uint32_t)b);
+  return VS_OK;
+}
+
 struct DevBuf {
   void* p = nullptr;
   ~DevBuf() {
@@ -80,8 +100,9 @@ int vs_session_config(vs_session* s, vs_config* out) {
 
 int vs_session_save(vs_session* s, const char* path) {
   if (!s || !path) return fail_code(VS_ERR_ARG, "null argument");
-  std::vector<uint32_t> list;
+  std::vector<uint32_t> list, flagged;
   int rc = occupied_bricks(s, list);
+  if (rc == VS_OK) rc = flagged_bricks(s, flagged);
   if (rc) return rc;
   vs_config cfg = s->cfg;
   double T[16];
@@ -115,6 +136,8 @@ int vs_session_save(vs_session* s, const char* path) {
             write_all(f, T, sizeof(T)) && write_all(f, &fr, 4) && write_all(f, &tr, 4) && write_all(f, &n64, 8) &&
             write_all(f, list.data(), n * 4) && write_all(f, words.data(), words.size()) &&
             write_all(f, cols.data(), cols.size() * 4);
+  const uint64_t m64 = flagged.size();
+  ok = ok && write_all(f, &m64, 8) && write_all(f, flagged.data(), flagged.size() * 4);
   ok = (std::fclose(f) == 0) && ok;
   if (!ok) return fail_code(VS_ERR_ARG, std::string("write failed: ") + path);
   return VS_OK;
@@ -149,10 +172,23 @@ int vs_session_load(const char* path, vs_session** out) {
   std::vector<uint32_t> cols(cfg.color ? n * kBrickVox : 0);
   ok = read_all(f, list.data(), n * 4) && read_all(f, words.data(), words.size()) &&
        read_all(f, cols.data(), cols.size() * 4);
+  // the flagged set is optional (absent: nothing flagged)
+  std::vector<uint32_t> flagged;
+  uint64_t m = 0;
+  if (ok && read_all(f, &m, 8)) {
+    if (m > nbr) ok = false;
+    if (ok) {
+      flagged.resize(m);
+      ok = read_all(f, flagged.data(), m * 4);
+    }
+  }
   std::fclose(f);
   if (!ok) return fail_code(VS_ERR_ARG, "truncated snapshot");
   for (uint64_t i = 0; i < n; i++)
     if (list[i] >= nbr || (i && list[i] <= list[i - 1])) return fail_code(VS_ERR_ARG, "corrupt sub-cube index list");
+  for (uint64_t i = 0; i < m; i++)
+    if (flagged[i] >= nbr || (i && flagged[i] <= flagged[i - 1]))
+      return fail_code(VS_ERR_ARG, "corrupt flagged sub-cube list");
   vs_session* s = nullptr;
   int rc = vs_session_create(&cfg, &s);
   if (rc) return rc;
@@ -176,6 +212,15 @@ int vs_session_load(const char* path, vs_session** out) {
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(s->stream);
     if (e != cudaSuccess) return bail(cuda_fail_code(e, "snapshot scatter"), "");
+  }
+  if (m) {
+    // activation stamp 1, and flag 1 on the flagged sub-cubes
+    std::vector<uint32_t> flags(nbr, 0u);
+    for (uint32_t b : flagged) flags[b] = 1u;
+    const uint32_t stamp = 1u;
+    cudaError_t e = cudaMemcpy(s->h.brick_flag, flags.data(), nbr * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->h.brick_count + 2, &stamp, 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return bail(cuda_fail_code(e, "snapshot flags"), "");
   }
   rc = vs_set_pose(s, T);
   if (rc) return bail(rc, "");

@@ -151,6 +151,10 @@ _SIGS = {
     "vs_get_device_buffer": (_I, [_P, _I, ctypes.POINTER(_P)]),
     "vs_integrate_depth_color": (_I, [_P, _P, _P, _I, _I, _P, _P]),
     "vs_render_maps_color": (_I, [_P, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P, _P]),
+    "vs_render_maps_scene": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "vs_render_view_scene": (_I, [_P, _I, _I, _P, _P, _P, _P, _P, _P, _P, _P]),
+    "vs_render_view": (_I, [_P, _I, _I, _P, _P, _P, _P, _I, _P, _P, _P, _P]),
+    "vs_update_valid_volume": (_I, [_P, _P, _I, ctypes.POINTER(ctypes.c_uint32)]),
     "vs_set_color_frame": (_I, [_P, _P, _I]),
     "vs_get_color_volume": (_I, [_P, _P]),
     "vs_set_color_volume": (_I, [_P, _P]),
@@ -355,6 +359,44 @@ class Session:
         _check(self.lib.vs_render_maps_color(self.h, w, h, _ptr(T_gc_dev), _ptr(T_cg_dev), _ptr(c), _ptr(l), level,
                                              _ptr(depth_dev), _ptr(vertex_dev), _ptr(normal_dev), _ptr(img_dev),
                                              _ptr(rgb_dev)))
+
+    def rmis_render_maps_for_scene(self, T_gc_dev, T_cg_dev, cam_cen, light, depth_dev, vertex_dev, normal_dev,
+                                   img_dev, rgb_dev=None):
+        """the scene ray-cast at level 0; vertex_dev None: the form without a
+        vertex map (trilinear colour), else the one with it (nearest colour)"""
+        w, h = self.levels[0][0], self.levels[0][1]
+        c = np.ascontiguousarray(cam_cen, dtype=np.float32)
+        l = np.ascontiguousarray(light, dtype=np.float32)
+        if vertex_dev is None:
+            _check(self.lib.vs_render_view_scene(self.h, w, h, _ptr(T_gc_dev), _ptr(T_cg_dev), _ptr(c), _ptr(l),
+                                                 _ptr(depth_dev), _ptr(normal_dev), _ptr(img_dev), _ptr(rgb_dev)))
+        else:
+            _check(self.lib.vs_render_maps_scene(self.h, w, h, _ptr(T_gc_dev), _ptr(T_cg_dev), _ptr(c), _ptr(l),
+                                                 _ptr(depth_dev), _ptr(vertex_dev), _ptr(normal_dev), _ptr(img_dev),
+                                                 _ptr(rgb_dev)))
+
+    def rmi_render_view(self, level, T_gc_dev, T_cg_dev, cam_cen, light, depth_dev, normal_dev, img_dev,
+                        rgb_dev=None):
+        """the object ray-cast without a vertex map: global normals, white background"""
+        w, h = self.levels[level][0], self.levels[level][1]
+        c = np.ascontiguousarray(cam_cen, dtype=np.float32)
+        l = np.ascontiguousarray(light, dtype=np.float32)
+        _check(self.lib.vs_render_view(self.h, w, h, _ptr(T_gc_dev), _ptr(T_cg_dev), _ptr(c), _ptr(l), level,
+                                       _ptr(depth_dev), _ptr(normal_dev), _ptr(img_dev), _ptr(rgb_dev)))
+
+    def uvv_update_valid_volume(self, valid):
+        """valid: host array of dim[0]*dim[1]*dim[2] bytes (x fastest, 0 =
+        outside) or an 8-byte aligned device pointer (int); returns the number
+        of sub-cubes reset"""
+        n = ctypes.c_uint32(0)
+        if isinstance(valid, int):
+            _check(self.lib.vs_update_valid_volume(self.h, _ptr(valid), 0, ctypes.byref(n)))
+        else:
+            m = np.ascontiguousarray(valid, dtype=np.uint8).reshape(-1)
+            if m.size != self.cfg.dim[0] * self.cfg.dim[1] * self.cfg.dim[2]:
+                raise ValueError("valid volume size differs from the session's")
+            _check(self.lib.vs_update_valid_volume(self.h, _ptr(m), 1, ctypes.byref(n)))
+        return int(n.value)
 
     def set_color_frame(self, rgb):
         """planar uint8 (3, height, width) host array, or a device pointer (int)"""
