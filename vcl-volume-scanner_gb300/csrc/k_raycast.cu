@@ -57,8 +57,22 @@ struct Vol {
   const uint32_t* occ1;  // 32^3-voxel cells
   const uint32_t* occ2;  // 128^3-voxel cells
   int dim[3];
-  int nb[3];
   int nc1[3], nc2[3];
+  uint32_t sy, sz;  // word strides of one brick row / one brick slab: 512 nb[0], 512 nb[0] nb[1]
+  // The word index of voxel (x, y, z) >= 0 is the sum of one term per axis
+  // (brick part + offset inside the brick), in 32 bits (volumes of at most
+  // 1024^3 voxels have fewer than 2^30 words).  Stencils compute each axis
+  // term once and add them.
+  __device__ inline uint32_t wx(int x) const { return (((uint32_t)x >> 3) << 9) + ((uint32_t)x & 7u); }
+  __device__ inline uint32_t wy(int y) const { return ((uint32_t)y >> 3) * sy + (((uint32_t)y & 7u) << 3); }
+  __device__ inline uint32_t wz(int z) const { return ((uint32_t)z >> 3) * sz + (((uint32_t)z & 7u) << 6); }
+  // the value of word i, and whether its weight is > 0 (a voxel of an
+  // unoccupied brick has weight 0, so the weight alone decides)
+  __device__ inline bool word_ok(uint32_t i, float& t) const {
+    uint32_t w;
+    S::decode(__ldg(v + i), t, w);
+    return w != 0u;
+  }
   __device__ inline bool cell_set(const uint32_t* bits, const int* nc, int shift, int x, int y, int z) const {
     const uint32_t c = ((uint32_t)(z >> shift) * (uint32_t)nc[1] + (uint32_t)(y >> shift)) * (uint32_t)nc[0] +
                        (uint32_t)(x >> shift);
@@ -74,8 +88,8 @@ struct Vol {
   // position lies in an occupied 32^3 cell that the ray leaves after about k
   // steps; the caller need not ask again before then (asking late only
   // delays a run, it never changes a sample).
+  // A NaN coordinate fails every comparison below and gives 0.
   __device__ inline int free_run(F3 p, F3 inc) const {
-    if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return 0;
     const float d = 0.05f;
     const float pa[3] = {p.x, p.y, p.z}, ia[3] = {inc.x, inc.y, inc.z};
     const float ra[3] = {__fdividef(1.0f, inc.x), __fdividef(1.0f, inc.y), __fdividef(1.0f, inc.z)};
@@ -97,7 +111,8 @@ struct Vol {
           t = fmaxf(t, ia[a] < 0.0f ? (hi + d - pa[a]) * ra[a] : 1e30f);
       }
     } else {
-      const int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
+      // inside: every coordinate > -0.5, where ROUNDF is (int)(p + 0.5)
+      const int x = (int)(p.x + 0.5f), y = (int)(p.y + 0.5f), z = (int)(p.z + 0.5f);
       int size = 32;
       if (!cell_set(occ2, nc2, 7, x, y, z))
         size = 128;
@@ -121,36 +136,22 @@ struct Vol {
     return m > 0 ? m : 0;
   }
 
-  __device__ inline bool occupied(int x, int y, int z) const {
-    const uint32_t b = ((uint32_t)(z >> 3) * (uint32_t)nb[1] + (uint32_t)(y >> 3)) * (uint32_t)nb[0] + (uint32_t)(x >> 3);
-    return (__ldg(occ + (b >> 5)) >> (b & 31)) & 1u;
-  }
-  // d_gtvu_Get_TSDF_Value_Uninterpolated: nearest voxel (ROUNDF), weight > 0
+  // d_gtvu_Get_TSDF_Value_Uninterpolated: nearest voxel (ROUNDF), weight > 0.
+  // ROUNDF(p) is negative for every p <= -0.5 and equals (int)(p + 0.5) for
+  // every p > -0.5 (both branches give 0 on (-0.5, 0)), so one comparison per
+  // coordinate decides the lower bound, and a NaN coordinate fails it too.
   __device__ inline bool gtvu(F3 p, float& out) const {
     out = 1.0f;
-    if (isnan(p.x) || isnan(p.y) || isnan(p.z)) return false;
-    int x = roundf_ref(p.x), y = roundf_ref(p.y), z = roundf_ref(p.z);
-    if (x < 0 || x >= dim[0] || y < 0 || y >= dim[1] || z < 0 || z >= dim[2]) return false;
-    if (!occupied(x, y, z)) return false;
+    if (!(p.x > -0.5f && p.y > -0.5f && p.z > -0.5f)) return false;
+    const int x = (int)(p.x + 0.5f), y = (int)(p.y + 0.5f), z = (int)(p.z + 0.5f);
+    if (x >= dim[0] || y >= dim[1] || z >= dim[2]) return false;
+    const uint32_t i = wx(x) + wy(y) + wz(z);
+    // brick index = i / 512
+    if (!((__ldg(occ + (i >> 14)) >> ((i >> 9) & 31u)) & 1u)) return false;
     float t;
-    uint32_t w;
-    S::decode(__ldg(v + brick_word_index(x, y, z, nb)), t, w);
-    if (w == 0u) return false;
+    if (!word_ok(i, t)) return false;
     out = t;
     return true;
-  }
-  // a voxel read issued without a test in front of it: out-of-range
-  // coordinates read voxel 0 and report invalid, so a group of reads goes to
-  // the memory system back to back instead of one after another.  A voxel of
-  // an unoccupied brick has weight 0, so the weight alone decides (the same
-  // answer as at()).
-  __device__ inline bool at_any(int x, int y, int z, float& out) const {
-    const bool in = x >= 0 && x < dim[0] && y >= 0 && y < dim[1] && z >= 0 && z < dim[2];
-    float t;
-    uint32_t w;
-    S::decode(__ldg(v + (in ? brick_word_index(x, y, z, nb) : 0)), t, w);
-    out = t;
-    return in && w != 0u;
   }
   // d_gtvi_Get_TSDF_Value_Interpolated (offset = floor, see the oracle); the
   // eight reads have no side effects, so reading all of them before the
@@ -161,15 +162,20 @@ struct Vol {
     float fx = floorf(p.x), fy = floorf(p.y), fz = floorf(p.z);
     int ox = (int)fx, oy = (int)fy, oz = (int)fz;
     float rx = p.x - fx, ry = p.y - fy, rz = p.z - fz;
+    // the eight corners are in range iff both values of every axis are; an
+    // out-of-range value is clamped for its (discarded) read
+    bool ok = ox >= 0 && ox + 1 < dim[0] && oy >= 0 && oy + 1 < dim[1] && oz >= 0 && oz + 1 < dim[2];
+    const int cx = min(max(ox, 0), dim[0] - 2), cy = min(max(oy, 0), dim[1] - 2), cz = min(max(oz, 0), dim[2] - 2);
+    const uint32_t x0 = wx(cx), x1 = wx(cx + 1), y0 = wy(cy), y1 = wy(cy + 1), z0 = wz(cz), z1 = wz(cz + 1);
     float f0, f1, f2, f3_, b0, b1, b2, b3;
-    bool ok = at_any(ox, oy, oz, f0);
-    ok &= at_any(ox + 1, oy, oz, f1);
-    ok &= at_any(ox, oy + 1, oz, f2);
-    ok &= at_any(ox + 1, oy + 1, oz, f3_);
-    ok &= at_any(ox, oy, oz + 1, b0);
-    ok &= at_any(ox + 1, oy, oz + 1, b1);
-    ok &= at_any(ox, oy + 1, oz + 1, b2);
-    ok &= at_any(ox + 1, oy + 1, oz + 1, b3);
+    ok &= word_ok(z0 + y0 + x0, f0);
+    ok &= word_ok(z0 + y0 + x1, f1);
+    ok &= word_ok(z0 + y1 + x0, f2);
+    ok &= word_ok(z0 + y1 + x1, f3_);
+    ok &= word_ok(z1 + y0 + x0, b0);
+    ok &= word_ok(z1 + y0 + x1, b1);
+    ok &= word_ok(z1 + y1 + x0, b2);
+    ok &= word_ok(z1 + y1 + x1, b3);
     if (!ok) return false;
     float inf = (1.0f - ry) * ((1.0f - rx) * f0 + rx * f1) + ry * ((1.0f - rx) * f2 + rx * f3_);
     float inb = (1.0f - ry) * ((1.0f - rx) * b0 + rx * b1) + ry * ((1.0f - rx) * b2 + rx * b3);
@@ -192,17 +198,23 @@ __device__ bool surface_normal(const Vol<S>& V, const SessionDev& s, F3 p3d, F3&
   const int dx2[12] = {0, 1, -1, 0, 1, 2, -1, 0, 1, 2, 0, 1};
   const int dy2[12] = {-1, -1, 0, 0, 0, 0, 1, 1, 1, 1, 2, 2};
   // all 32 reads are issued before any validity test (no side effects, so
-  // the result equals the reference's read-and-return-early order)
+  // the result equals the reference's read-and-return-early order).  The
+  // stencil spans o - 1 .. o + 2 on every axis and uses each of those values,
+  // so it is in range iff o - 1 >= 0 and o + 2 < dim on all three axes.
+  bool ok = ox >= 1 && ox + 2 < V.dim[0] && oy >= 1 && oy + 2 < V.dim[1] && oz >= 1 && oz + 2 < V.dim[2];
+  const int cx = min(max(ox, 1), V.dim[0] - 3), cy = min(max(oy, 1), V.dim[1] - 3), cz = min(max(oz, 1), V.dim[2] - 3);
+  uint32_t X[4], Y[4], Z[4];
+#pragma unroll
+  for (int k = 0; k < 4; k++) X[k] = V.wx(cx - 1 + k), Y[k] = V.wy(cy - 1 + k), Z[k] = V.wz(cz - 1 + k);
   float fm[4], fr[12], bk[12], bm[4];
-  bool ok = true;
 #pragma unroll
-  for (int i = 0; i < 4; i++) ok &= V.at_any(ox + dx1[i], oy + dy1[i], oz - 1, fm[i]);
+  for (int i = 0; i < 4; i++) ok &= V.word_ok(Z[0] + Y[1 + dy1[i]] + X[1 + dx1[i]], fm[i]);
 #pragma unroll
-  for (int i = 0; i < 12; i++) ok &= V.at_any(ox + dx2[i], oy + dy2[i], oz, fr[i]);
+  for (int i = 0; i < 12; i++) ok &= V.word_ok(Z[1] + Y[1 + dy2[i]] + X[1 + dx2[i]], fr[i]);
 #pragma unroll
-  for (int i = 0; i < 12; i++) ok &= V.at_any(ox + dx2[i], oy + dy2[i], oz + 1, bk[i]);
+  for (int i = 0; i < 12; i++) ok &= V.word_ok(Z[2] + Y[1 + dy2[i]] + X[1 + dx2[i]], bk[i]);
 #pragma unroll
-  for (int i = 0; i < 4; i++) ok &= V.at_any(ox + dx1[i], oy + dy1[i], oz + 2, bm[i]);
+  for (int i = 0; i < 4; i++) ok &= V.word_ok(Z[3] + Y[1 + dy1[i]] + X[1 + dx1[i]], bm[i]);
   if (!ok) return false;
   float a4[4], b4[4], a2[2], b2[2], gx, gy, gz;
   a4[0] = (1.0f - rz) * fr[2] + rz * bk[2];
@@ -313,14 +325,17 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
         m = 0;
       }
       // the loop above would stop at iteration cap + 1: run at most cap - it
-      // steps here, then stop as it would
+      // steps here, then stop as it would.  total only grows (sn > 0), so it
+      // passed total_max inside the run iff it is past it at the end, and the
+      // ray then ends without a hit whichever step it was.
       const bool capped = m > cap - it;
       const int run = capped ? cap - it : m;
+#pragma unroll 4
       for (int k = 0; k < run; k++) {
         vs = add(vs, inc);
         total += sn;
-        if (total > total_max) return false;
       }
+      if (total > total_max) return false;
       it += run;
       if (capped) return false;
     }
@@ -402,7 +417,9 @@ __device__ inline Vol<S> volume_of(const SessionDev& s) {
   V.occ = s.occ;
   V.occ1 = s.occ1;
   V.occ2 = s.occ2;
-  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nb[k] = s.nb[k], V.nc1[k] = s.nc1[k], V.nc2[k] = s.nc2[k];
+  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nc1[k] = s.nc1[k], V.nc2[k] = s.nc2[k];
+  V.sy = (uint32_t)s.nb[0] << 9;
+  V.sz = ((uint32_t)s.nb[0] * (uint32_t)s.nb[1]) << 9;
   return V;
 }
 
@@ -460,14 +477,14 @@ __device__ uint32_t trilinear_color(const Vol<S>& V, const SessionDev& s, F3 pg)
   const int ox = (int)fx, oy = (int)fy, oz = (int)fz;
   const float rx = v.x - fx, ry = v.y - fy, rz = v.z - fz;
   float tdummy;
-  bool ok = true;
+  bool ok = ox >= 0 && ox + 1 < V.dim[0] && oy >= 0 && oy + 1 < V.dim[1] && oz >= 0 && oz + 1 < V.dim[2];
+  const int cx = min(max(ox, 0), V.dim[0] - 2), cy = min(max(oy, 0), V.dim[1] - 2), cz = min(max(oz, 0), V.dim[2] - 2);
+  const uint32_t X[2] = {V.wx(cx), V.wx(cx + 1)}, Y[2] = {V.wy(cy), V.wy(cy + 1)}, Z[2] = {V.wz(cz), V.wz(cz + 1)};
   uint32_t c[8];
 #pragma unroll
   for (int i = 0; i < 8; i++) {
-    const int x = ox + (i & 1), y = oy + ((i >> 1) & 1), z = oz + (i >> 2);
-    const bool in = x >= 0 && x < V.dim[0] && y >= 0 && y < V.dim[1] && z >= 0 && z < V.dim[2];
-    const size_t w = in ? brick_word_index(x, y, z, V.nb) : 0;
-    ok &= V.at_any(x, y, z, tdummy);
+    const uint32_t w = Z[i >> 2] + Y[(i >> 1) & 1] + X[i & 1];
+    ok &= V.word_ok(w, tdummy);
     c[i] = __ldg(s.col + w);
   }
   if (!ok) return 0u;
@@ -500,9 +517,11 @@ __device__ uint32_t nearest_color(const Vol<S>& V, const SessionDev& s, F3 pg) {
   pos_in_voxel(pg, s, v);
   if (isnan(v.x) || isnan(v.y) || isnan(v.z)) return 0u;
   const int x = roundf_ref(v.x), y = roundf_ref(v.y), z = roundf_ref(v.z);
+  if (x < 0 || x >= V.dim[0] || y < 0 || y >= V.dim[1] || z < 0 || z >= V.dim[2]) return 0u;
+  const uint32_t w = V.wx(x) + V.wy(y) + V.wz(z);
   float t;
-  if (!V.at_any(x, y, z, t)) return 0u;
-  return __ldg(s.col + brick_word_index(x, y, z, V.nb));
+  if (!V.word_ok(w, t)) return 0u;
+  return __ldg(s.col + w);
 }
 
 // phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
