@@ -427,8 +427,8 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
         // occupancy cells around it, stay occupied
         if (q.occ) {
           set_bit_once(q.occ, b);
-          set_bit_once(q.occ1, occ_cell(bx, by, bz, 2, q.nc1));
-          set_bit_once(q.occ2, occ_cell(bx, by, bz, 4, q.nc2));
+          set_bit_once(q.occ1, occ_cell(bx, by, bz, kOcc1Shift, q.nc1));
+          set_bit_once(q.occ2, occ_cell(bx, by, bz, kOcc2Shift, q.nc2));
         }
       }
     }
@@ -497,8 +497,8 @@ __global__ void k_occupancy(const SessionDev* __restrict__ s) {
     if (lane == 0 && m) {
       const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / ((size_t)nb0 * nb1));
       set_bit_once(s->occ, (uint32_t)b);
-      set_bit_once(s->occ1, occ_cell(bx, by, bz, 2, s->nc1));
-      set_bit_once(s->occ2, occ_cell(bx, by, bz, 4, s->nc2));
+      set_bit_once(s->occ1, occ_cell(bx, by, bz, kOcc1Shift, s->nc1));
+      set_bit_once(s->occ2, occ_cell(bx, by, bz, kOcc2Shift, s->nc2));
     }
   }
 }

@@ -54,8 +54,8 @@ template <class S>
 struct Vol {
   const typename S::word* v;
   const uint32_t* occ;
-  const uint32_t* occ1;  // 32^3-voxel cells
-  const uint32_t* occ2;  // 128^3-voxel cells
+  const uint32_t* occ1;  // cells of 2^kOcc1Shift bricks per axis
+  const uint32_t* occ2;  // cells of 2^kOcc2Shift bricks per axis
   int dim[3];
   int nc1[3], nc2[3];
   uint32_t sy, sz;  // word strides of one brick row / one brick slab: 512 nb[0], 512 nb[0] nb[1]
@@ -85,7 +85,7 @@ struct Vol {
   // rounding of the position accumulated over a run (at most 64 steps of
   // float additions, under 1e-2 voxel for coordinates below 2048) or of the
   // approximate reciprocals of the increment.  A negative result -k says the
-  // position lies in an occupied 32^3 cell that the ray leaves after about k
+  // position lies in an occupied occ1 cell that the ray leaves after about k
   // steps; the caller need not ask again before then (asking late only
   // delays a run, it never changes a sample).
   // A NaN coordinate fails every comparison below and gives 0.
@@ -113,10 +113,10 @@ struct Vol {
     } else {
       // inside: every coordinate > -0.5, where ROUNDF is (int)(p + 0.5)
       const int x = (int)(p.x + 0.5f), y = (int)(p.y + 0.5f), z = (int)(p.z + 0.5f);
-      int size = 32;
-      if (!cell_set(occ2, nc2, 7, x, y, z))
-        size = 128;
-      else if (cell_set(occ1, nc1, 5, x, y, z))
+      int size = 8 << kOcc1Shift;
+      if (!cell_set(occ2, nc2, kOcc2Shift + 3, x, y, z))
+        size = 8 << kOcc2Shift;
+      else if (cell_set(occ1, nc1, kOcc1Shift + 3, x, y, z))
         occupied_cell = true;
       const int c[3] = {x & ~(size - 1), y & ~(size - 1), z & ~(size - 1)};
       t = 1e30f;
@@ -291,21 +291,19 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
   const int cap = 4 * (int)total_max + 64;
   int it = 0;
   int recheck = 0;  // full steps before the next free-space test
-  while (state != BEHIND) {
-    if (++it > cap) return false;
-    if (state == COARSE)
-      step = step_scale;
-    else
-      step = (tsdf > 0.0f) ? fmaxf(step_scale * tsdf, 1.0f) : fminf(step_scale * tsdf, -1.0f);
-    vs = add(vs, scale(step, rd));
-    total += step;
-    if (total > total_max) break;
-    V.gtvu(vs, tsdf);
-    if (tsdf > -1.0f && tsdf < 1.0f) {
+  // The reference's loop, reordered: each pass handles the sample just read
+  // (none for the start sample), then advances.  While samples read 1 (no
+  // value, or free space) neither the state nor the step changes, so those
+  // steps run in a tight loop with a fixed increment, and runs that are
+  // certain to read no value replay their float additions without reads.
+  bool first = true;
+  for (;;) {
+    if (!first && tsdf > -1.0f && tsdf < 1.0f) {
       V.gtvi(vs, tsdf);
       if (tsdf < 0.0f) {
-        if (state == COARSE) break;
+        if (state == COARSE) return false;
         state = BEHIND;
+        break;
       } else if (tsdf == 0.0f) {
         p3d = pos_in_world(vs, s);
         return true;
@@ -313,31 +311,47 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
         state = FINE;
       }
     }
-    if (tsdf == 1.0f && state != BEHIND && --recheck < 0) {
-      // While samples read "no value" (TSDF 1) the state and the step stay as
-      // they are, so the steps of a free-space run are replayed with the same
-      // float operations as the loop above, without the volume reads.
+    first = false;
+    if (tsdf == 1.0f) {
       const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
       const F3 inc = scale(sn, rd);
-      int m = V.free_run(vs, inc);
-      if (m < 0) {
-        recheck = -m;
-        m = 0;
-      }
-      // the loop above would stop at iteration cap + 1: run at most cap - it
-      // steps here, then stop as it would.  total only grows (sn > 0), so it
-      // passed total_max inside the run iff it is past it at the end, and the
-      // ray then ends without a hit whichever step it was.
-      const bool capped = m > cap - it;
-      const int run = capped ? cap - it : m;
+      for (;;) {
+        if (--recheck < 0) {
+          int m = V.free_run(vs, inc);
+          if (m < 0) {
+            recheck = -m;
+            m = 0;
+          }
+          // the loop would stop at iteration cap + 1: run at most cap - it
+          // steps here, then stop as it would.  total only grows (sn > 0),
+          // so it passed total_max inside the run iff it is past it at the
+          // end, and the ray then ends without a hit whichever step it was.
+          const bool capped = m > cap - it;
+          const int run = capped ? cap - it : m;
 #pragma unroll 4
-      for (int k = 0; k < run; k++) {
+          for (int k = 0; k < run; k++) {
+            vs = add(vs, inc);
+            total += sn;
+          }
+          if (total > total_max) return false;
+          it += run;
+          if (capped) return false;
+        }
+        if (++it > cap) return false;
         vs = add(vs, inc);
         total += sn;
+        if (total > total_max) return false;
+        V.gtvu(vs, tsdf);
+        if (tsdf != 1.0f) break;
       }
+    } else {
+      if (++it > cap) return false;
+      step = (state == COARSE) ? step_scale
+                               : ((tsdf > 0.0f) ? fmaxf(step_scale * tsdf, 1.0f) : fminf(step_scale * tsdf, -1.0f));
+      vs = add(vs, scale(step, rd));
+      total += step;
       if (total > total_max) return false;
-      it += run;
-      if (capped) return false;
+      V.gtvu(vs, tsdf);
     }
   }
   if (state == BEHIND) {

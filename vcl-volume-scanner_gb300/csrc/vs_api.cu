@@ -95,8 +95,8 @@ void fill_geometry(const vs_config* c, SessionDev& h) {
   for (int k = 0; k < 3; k++) {
     h.dim[k] = c->dim[k];
     h.nb[k] = c->dim[k] / 8;
-    h.nc1[k] = (h.nb[k] + 3) / 4;
-    h.nc2[k] = (h.nb[k] + 15) / 16;
+    h.nc1[k] = (h.nb[k] + (1 << kOcc1Shift) - 1) >> kOcc1Shift;
+    h.nc2[k] = (h.nb[k] + (1 << kOcc2Shift) - 1) >> kOcc2Shift;
     h.origin[k] = c->origin[k];
   }
   h.vox = c->voxel_size;

@@ -82,7 +82,7 @@ struct SessionDev {
   uint32_t* brick_list;          // active bricks of this frame
   uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame), [2] activation stamp
   uint32_t* occ;                 // 1 bit per brick: some voxel has weight > 0 (NULL: not kept)
-  uint32_t* occ1;                // 1 bit per 4^3 bricks (32^3 voxels): some brick occupied
+  uint32_t* occ1;                // 1 bit per occ1 cell (default 4^3 bricks): some brick occupied
   uint32_t* occ2;                // 1 bit per 16^3 bricks (128^3 voxels)
   int nc1[3], nc2[3];            // cells per axis of occ1 / occ2
   // ICP scratch
@@ -201,8 +201,20 @@ __device__ inline F3 pos_in_world(F3 v, const SessionDev& s) {
 __host__ __device__ inline uint32_t pack_rgb(uint32_t r, uint32_t g, uint32_t b) { return r | (g << 8) | (b << 16); }
 __host__ __device__ inline uint32_t rgb_channel(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
-// occupancy cell index of brick (bx, by, bz) at level `shift` (2: 4^3
-// bricks, 4: 16^3 bricks) in a grid of nc cells per axis
+// The two coarse occupancy levels: cells of 2^kOcc1Shift and 2^kOcc2Shift
+// bricks per axis (32^3 and 128^3 voxels by default).  Only the ray-cast's
+// free-space skipping reads them, so they change speed, never a result.
+#ifndef VS_OCC1_BRICK_SHIFT
+#define VS_OCC1_BRICK_SHIFT 2
+#endif
+#ifndef VS_OCC2_BRICK_SHIFT
+#define VS_OCC2_BRICK_SHIFT 4
+#endif
+constexpr int kOcc1Shift = VS_OCC1_BRICK_SHIFT;
+constexpr int kOcc2Shift = VS_OCC2_BRICK_SHIFT;
+
+// occupancy cell index of brick (bx, by, bz) at level `shift` (kOcc1Shift or
+// kOcc2Shift) in a grid of nc cells per axis
 __host__ __device__ inline uint32_t occ_cell(int bx, int by, int bz, int shift, const int* nc) {
   return ((uint32_t)(bz >> shift) * (uint32_t)nc[1] + (uint32_t)(by >> shift)) * (uint32_t)nc[0] +
          (uint32_t)(bx >> shift);
