@@ -291,19 +291,21 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
   const int cap = 4 * (int)total_max + 64;
   int it = 0;
   int recheck = 0;  // full steps before the next free-space test
-  // The reference's loop, reordered: each pass handles the sample just read
-  // (none for the start sample), then advances.  While samples read 1 (no
-  // value, or free space) neither the state nor the step changes, so those
-  // steps run in a tight loop with a fixed increment, and runs that are
-  // certain to read no value replay their float additions without reads.
-  bool first = true;
-  for (;;) {
-    if (!first && tsdf > -1.0f && tsdf < 1.0f) {
+  while (state != BEHIND) {
+    if (++it > cap) return false;
+    if (state == COARSE)
+      step = step_scale;
+    else
+      step = (tsdf > 0.0f) ? fmaxf(step_scale * tsdf, 1.0f) : fminf(step_scale * tsdf, -1.0f);
+    vs = add(vs, scale(step, rd));
+    total += step;
+    if (total > total_max) break;
+    V.gtvu(vs, tsdf);
+    if (tsdf > -1.0f && tsdf < 1.0f) {
       V.gtvi(vs, tsdf);
       if (tsdf < 0.0f) {
-        if (state == COARSE) return false;
+        if (state == COARSE) break;
         state = BEHIND;
-        break;
       } else if (tsdf == 0.0f) {
         p3d = pos_in_world(vs, s);
         return true;
@@ -311,47 +313,31 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
         state = FINE;
       }
     }
-    first = false;
-    if (tsdf == 1.0f) {
+    if (tsdf == 1.0f && state != BEHIND && --recheck < 0) {
+      // While samples read "no value" (TSDF 1) the state and the step stay as
+      // they are, so the steps of a free-space run are replayed with the same
+      // float operations as the loop above, without the volume reads.
       const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
       const F3 inc = scale(sn, rd);
-      for (;;) {
-        if (--recheck < 0) {
-          int m = V.free_run(vs, inc);
-          if (m < 0) {
-            recheck = -m;
-            m = 0;
-          }
-          // the loop would stop at iteration cap + 1: run at most cap - it
-          // steps here, then stop as it would.  total only grows (sn > 0),
-          // so it passed total_max inside the run iff it is past it at the
-          // end, and the ray then ends without a hit whichever step it was.
-          const bool capped = m > cap - it;
-          const int run = capped ? cap - it : m;
+      int m = V.free_run(vs, inc);
+      if (m < 0) {
+        recheck = -m;
+        m = 0;
+      }
+      // the loop above would stop at iteration cap + 1: run at most cap - it
+      // steps here, then stop as it would.  total only grows (sn > 0), so it
+      // passed total_max inside the run iff it is past it at the end, and the
+      // ray then ends without a hit whichever step it was.
+      const bool capped = m > cap - it;
+      const int run = capped ? cap - it : m;
 #pragma unroll 4
-          for (int k = 0; k < run; k++) {
-            vs = add(vs, inc);
-            total += sn;
-          }
-          if (total > total_max) return false;
-          it += run;
-          if (capped) return false;
-        }
-        if (++it > cap) return false;
+      for (int k = 0; k < run; k++) {
         vs = add(vs, inc);
         total += sn;
-        if (total > total_max) return false;
-        V.gtvu(vs, tsdf);
-        if (tsdf != 1.0f) break;
       }
-    } else {
-      if (++it > cap) return false;
-      step = (state == COARSE) ? step_scale
-                               : ((tsdf > 0.0f) ? fmaxf(step_scale * tsdf, 1.0f) : fminf(step_scale * tsdf, -1.0f));
-      vs = add(vs, scale(step, rd));
-      total += step;
       if (total > total_max) return false;
-      V.gtvu(vs, tsdf);
+      it += run;
+      if (capped) return false;
     }
   }
   if (state == BEHIND) {
