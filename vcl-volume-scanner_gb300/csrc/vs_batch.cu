@@ -9,6 +9,14 @@
 // before it reuses that step's buffers.  A step ends by gathering every
 // slot's pose head into one buffer that a single copy brings to the host.
 //
+// ICP runs as two independent launch sequences on two branches of the graph,
+// each over half of the sessions (split by pixel count).  Every ICP launch
+// ends with a tail in which only the blocks that close a session's iteration
+// (a reduction and an FP64 solve) still run; with two sequences in flight
+// the other sequence's blocks fill the SMs that the tail leaves idle.  A
+// session's sums do not depend on which sessions share its launch, so the
+// split changes no result.
+//
 // The graph depends only on the schedule it was captured for: the deepest
 // pyramid and the largest ICP iteration count per level among the sessions,
 // whether any session needs input normal maps, the reduction mode and the
@@ -46,6 +54,7 @@ struct Schedule {
 };
 
 constexpr int kRing = 2;
+constexpr int kIcpGroups = 2;  // concurrent ICP launch sequences
 
 }  // namespace
 
@@ -53,8 +62,12 @@ struct vs_batch {
   int device = 0;
   cudaStream_t stream = nullptr;
   BatchTable* d_tab = nullptr;
+  BatchTable* d_grp = nullptr;                 // kIcpGroups tables: the ICP groups
   void* d_heads = nullptr;                     // kMaxSlots pose heads
   BatchTable* h_tab[kRing] = {nullptr, nullptr};  // pinned
+  BatchTable* h_grp[kRing] = {nullptr, nullptr};  // pinned, kIcpGroups each
+  cudaStream_t side = nullptr;                 // second graph branch (ICP group 1)
+  cudaEvent_t fork = nullptr, join = nullptr;
   unsigned char* h_heads[kRing] = {nullptr, nullptr};  // pinned
   cudaEvent_t done[kRing] = {nullptr, nullptr};
   bool used[kRing] = {false, false};
@@ -81,11 +94,17 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
     if (k.timing) cudaEventRecordWithFlags(b->ev[i], st, cudaEventRecordExternal);
   };
   cudaMemcpyAsync(b->d_tab, b->h_tab[r], sizeof(BatchTable), cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(b->d_grp, b->h_grp[r], kIcpGroups * sizeof(BatchTable), cudaMemcpyHostToDevice, st);
   mark(0);
   launch_filter(b->d_tab, st);
   if (k.inmaps) launch_input_maps(b->d_tab, st);
   mark(1);
-  launch_icp(b->d_tab, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
+  cudaEventRecord(b->fork, st);
+  cudaStreamWaitEvent(b->side, b->fork, 0);
+  launch_icp(b->d_grp, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
+  launch_icp(b->d_grp + 1, k.levels, k.iters, k.reduce_mode, b->side, true, nullptr);
+  cudaEventRecord(b->join, b->side);
+  cudaStreamWaitEvent(st, b->join, 0);
   mark(2);
   launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
   mark(3);
@@ -176,6 +195,26 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
     dr[i] = ss[i]->d;
   }
   fill_batch_table(*b->h_tab[r], hr, dr, n, b->shape.ray_lx);
+  // ICP groups: largest sessions first, each to the group with fewer pixels
+  int order[kMaxSlots];
+  for (int i = 0; i < n; i++) order[i] = i;
+  auto px = [&](int i) { return (long long)hr[i]->lv[0].W * hr[i]->lv[0].H; };
+  std::stable_sort(order, order + n, [&](int a, int c) { return px(a) > px(c); });
+  const SessionDev* gh[kIcpGroups][kMaxSlots];
+  const SessionDev* gd[kIcpGroups][kMaxSlots];
+  int gn[kIcpGroups] = {0};
+  long long load[kIcpGroups] = {0};
+  for (int q = 0; q < n; q++) {
+    const int i = order[q];
+    int g = 0;
+    for (int j = 1; j < kIcpGroups; j++)
+      if (load[j] < load[g]) g = j;
+    gh[g][gn[g]] = hr[i];
+    gd[g][gn[g]] = dr[i];
+    gn[g]++;
+    load[g] += px(i);
+  }
+  for (int g = 0; g < kIcpGroups; g++) fill_batch_table(b->h_grp[r][g], gh[g], gd[g], gn[g], b->shape.ray_lx);
   cudaError_t e = cudaGraphLaunch(b->exec[r], st);
   if (e == cudaSuccess) e = cudaEventRecord(b->done[r], st);
   if (e != cudaSuccess) return cuda_fail_code(e, "batch step launch");
@@ -203,9 +242,14 @@ void free_batch(vs_batch* b) {
   for (int r = 0; r < kRing; r++) {
     if (b->done[r]) cudaEventDestroy(b->done[r]);
     if (b->h_tab[r]) cudaFreeHost(b->h_tab[r]);
+    if (b->h_grp[r]) cudaFreeHost(b->h_grp[r]);
     if (b->h_heads[r]) cudaFreeHost(b->h_heads[r]);
   }
   if (b->d_tab) cudaFree(b->d_tab);
+  if (b->d_grp) cudaFree(b->d_grp);
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->join) cudaEventDestroy(b->join);
+  if (b->side) cudaStreamDestroy(b->side);
   if (b->d_heads) cudaFree(b->d_heads);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
@@ -250,11 +294,18 @@ int vs_batch_create(vs_batch** out) {
   vs_batch* b = new vs_batch;
   cudaGetDevice(&b->device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaMalloc(&b->d_tab, sizeof(BatchTable));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_grp, kIcpGroups * sizeof(BatchTable));
+  if (e == cudaSuccess) e = cudaMemset(b->d_grp, 0, kIcpGroups * sizeof(BatchTable));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_heads, kMaxSlots * kPoseHeadBytes);
   for (int r = 0; r < kRing && e == cudaSuccess; r++) {
     e = cudaMallocHost(&b->h_tab[r], sizeof(BatchTable));
     if (e == cudaSuccess) e = cudaMallocHost(&b->h_heads[r], kMaxSlots * kPoseHeadBytes);
+    if (e == cudaSuccess) e = cudaMallocHost(&b->h_grp[r], kIcpGroups * sizeof(BatchTable));
+    if (e == cudaSuccess) std::memset(b->h_grp[r], 0, kIcpGroups * sizeof(BatchTable));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done[r], cudaEventDisableTiming);
     if (e == cudaSuccess) std::memset(b->h_tab[r], 0, sizeof(BatchTable));
   }
