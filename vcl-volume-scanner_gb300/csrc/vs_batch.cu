@@ -9,11 +9,11 @@
 // before it reuses that step's buffers.  A step ends by gathering every
 // slot's pose head into one buffer that a single copy brings to the host.
 //
-// ICP runs as two independent launch sequences on two branches of the graph,
-// each over half of the sessions (split by pixel count).  Every ICP launch
+// ICP runs as kIcpGroups independent launch sequences on branches of the
+// graph, each over a share of the sessions (split by pixel count).  Every ICP launch
 // ends with a tail in which only the blocks that close a session's iteration
-// (a reduction and an FP64 solve) still run; with two sequences in flight
-// the other sequence's blocks fill the SMs that the tail leaves idle.  A
+// (a reduction and an FP64 solve) still run; with several sequences in
+// flight the other sequences' blocks fill the SMs that the tail leaves idle.  A
 // session's sums do not depend on which sessions share its launch, so the
 // split changes no result.
 //
@@ -54,7 +54,10 @@ struct Schedule {
 };
 
 constexpr int kRing = 2;
-constexpr int kIcpGroups = 2;  // concurrent ICP launch sequences
+#ifndef VS_ICP_GROUPS
+#define VS_ICP_GROUPS 2
+#endif
+constexpr int kIcpGroups = VS_ICP_GROUPS;  // concurrent ICP launch sequences
 
 }  // namespace
 
@@ -66,8 +69,8 @@ struct vs_batch {
   void* d_heads = nullptr;                     // kMaxSlots pose heads
   BatchTable* h_tab[kRing] = {nullptr, nullptr};  // pinned
   BatchTable* h_grp[kRing] = {nullptr, nullptr};  // pinned, kIcpGroups each
-  cudaStream_t side = nullptr;                 // second graph branch (ICP group 1)
-  cudaEvent_t fork = nullptr, join = nullptr;
+  cudaStream_t side[kIcpGroups] = {};         // graph branches of ICP groups 1..
+  cudaEvent_t fork = nullptr, join[kIcpGroups] = {};
   unsigned char* h_heads[kRing] = {nullptr, nullptr};  // pinned
   cudaEvent_t done[kRing] = {nullptr, nullptr};
   bool used[kRing] = {false, false};
@@ -100,11 +103,13 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
   if (k.inmaps) launch_input_maps(b->d_tab, st);
   mark(1);
   cudaEventRecord(b->fork, st);
-  cudaStreamWaitEvent(b->side, b->fork, 0);
+  for (int g = 1; g < kIcpGroups; g++) cudaStreamWaitEvent(b->side[g], b->fork, 0);
   launch_icp(b->d_grp, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
-  launch_icp(b->d_grp + 1, k.levels, k.iters, k.reduce_mode, b->side, true, nullptr);
-  cudaEventRecord(b->join, b->side);
-  cudaStreamWaitEvent(st, b->join, 0);
+  for (int g = 1; g < kIcpGroups; g++) {
+    launch_icp(b->d_grp + g, k.levels, k.iters, k.reduce_mode, b->side[g], true, nullptr);
+    cudaEventRecord(b->join[g], b->side[g]);
+    cudaStreamWaitEvent(st, b->join[g], 0);
+  }
   mark(2);
   launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
   mark(3);
@@ -248,8 +253,10 @@ void free_batch(vs_batch* b) {
   if (b->d_tab) cudaFree(b->d_tab);
   if (b->d_grp) cudaFree(b->d_grp);
   if (b->fork) cudaEventDestroy(b->fork);
-  if (b->join) cudaEventDestroy(b->join);
-  if (b->side) cudaStreamDestroy(b->side);
+  for (int g = 1; g < kIcpGroups; g++) {
+    if (b->join[g]) cudaEventDestroy(b->join[g]);
+    if (b->side[g]) cudaStreamDestroy(b->side[g]);
+  }
   if (b->d_heads) cudaFree(b->d_heads);
   if (b->stream) cudaStreamDestroy(b->stream);
 }
@@ -294,9 +301,11 @@ int vs_batch_create(vs_batch** out) {
   vs_batch* b = new vs_batch;
   cudaGetDevice(&b->device);
   cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
-  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+  for (int g = 1; g < kIcpGroups && e == cudaSuccess; g++) {
+    e = cudaStreamCreateWithFlags(&b->side[g], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[g], cudaEventDisableTiming);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&b->d_tab, sizeof(BatchTable));
   if (e == cudaSuccess) e = cudaMalloc(&b->d_grp, kIcpGroups * sizeof(BatchTable));
   if (e == cudaSuccess) e = cudaMemset(b->d_grp, 0, kIcpGroups * sizeof(BatchTable));
