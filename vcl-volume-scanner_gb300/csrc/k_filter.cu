@@ -409,7 +409,7 @@ void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const 
     hb.ipost[i + 1] = hb.ipost[i] + (nm ? ipost : 0);
     hb.scan[i + 1] = hb.scan[i] + (nm ? h.levels : 0);
     for (int l = 0; l < kMaxLevels; l++)
-      hb.icp[l][i + 1] = hb.icp[l][i] + (l < h.levels ? icp_blocks(h.lv[l].W * h.lv[l].H) : 0);
+      hb.icp[l][i + 1] = hb.icp[l][i] + (l < h.levels ? icp_blocks(h.lv[l].W * h.lv[l].H, l) : 0);
     hb.ray[i + 1] = hb.ray[i] + ray;
   }
 }

@@ -659,12 +659,20 @@ void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st) {
   k_gather_heads<<<kMaxSlots, 32, 0, st>>>(bt, reinterpret_cast<uint32_t*>(out));
 }
 
+// pixels per ICP range at level 0 and at the coarser levels.  A range is
+// the unit between two block barriers and one partial write: long ranges
+// spend less of the launch in barriers and reductions, short ranges keep
+// more blocks busy on the small coarse levels (and on a lone session).
 #ifndef VS_ICP_PIXELS_PER_RANGE
-#define VS_ICP_PIXELS_PER_RANGE 512
+#define VS_ICP_PIXELS_PER_RANGE 2048
+#endif
+#ifndef VS_ICP_PIXELS_PER_RANGE_COARSE
+#define VS_ICP_PIXELS_PER_RANGE_COARSE 512
 #endif
 
-int icp_blocks(int npix) {
-  int b = (npix + VS_ICP_PIXELS_PER_RANGE - 1) / VS_ICP_PIXELS_PER_RANGE;
+int icp_blocks(int npix, int level) {
+  const int ppr = level == 0 ? VS_ICP_PIXELS_PER_RANGE : VS_ICP_PIXELS_PER_RANGE_COARSE;
+  int b = (npix + ppr - 1) / ppr;
   if (b < 1) b = 1;
   if (b > kIcpMaxBlocks) b = kIcpMaxBlocks;
   return b;

@@ -287,7 +287,7 @@ struct LaunchShape {
   int shade_blocks_per_sm = 0;
 };
 
-int icp_blocks(int npix);
+int icp_blocks(int npix, int level);
 int sm_count();
 void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n,
                       int ray_lx = 3);
