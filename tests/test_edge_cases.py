@@ -1,0 +1,104 @@
+"""Edge cases of the per-frame path: empty frames, ragged image sizes, a
+session losing tracking inside a batch, and the largest volume and image the
+library accepts.
+
+An empty frame (no valid depth) gives the ICP nothing to sum: the reference's
+Cholesky then fails on a zero pivot, the frame counts as lost, and nothing is
+integrated.  Image sizes that are not multiples of the kernels' tiles must
+give the oracle's results as any other size does."""
+import numpy as np
+import pytest
+
+import helpers
+import oracle_py as O
+import vs_scanner as V
+
+pytestmark = pytest.mark.gpu
+
+
+def _same_pose(T, oT):
+    return helpers.rot_err(T, oT) < 1e-4 and helpers.trans_err(T, oT) < 1e-4
+
+
+def test_empty_frame_is_lost_like_the_oracle(gpu):
+    c = helpers.make_case(width=160, height=120, dim=96, size=0.75, frames=4, seed=21)
+    frames = [c["depth"][0], c["depth"][1], np.zeros_like(c["depth"][2]), c["depth"][3]]
+    osess = O.Session(c["ocfg"])
+    with V.Session(c["cfg"]) as s:
+        for k, f in enumerate(frames):
+            w_before = s.volume()[1].copy()
+            T, tracked = s.scan_frame_host(f)
+            otracked = osess.frame(f)
+            assert tracked == otracked, k
+            assert _same_pose(T, osess.pose()), k
+            if k == 2:
+                assert not tracked
+                # nothing integrated on a lost frame
+                assert np.array_equal(s.volume()[1], w_before)
+        assert tracked  # the next frame tracks again from the last good pose
+
+
+@pytest.mark.parametrize("size", [(170, 130), (97, 75)])
+def test_ragged_image_sizes_match_the_oracle(gpu, size):
+    w, h = size
+    c = helpers.make_case(width=w, height=h, dim=96, size=0.75, frames=3, seed=22)
+    osess = O.Session(c["ocfg"])
+    with V.Session(c["cfg"]) as s:
+        for k in range(3):
+            T, tracked = s.scan_frame_host(c["depth"][k])
+            assert tracked == osess.frame(c["depth"][k])
+            assert _same_pose(T, osess.pose()), (k, size)
+        for l in range(len(s.levels)):
+            md = s.maps(l)["model_depth"]
+            om = osess.maps(l)["model_depth"]
+            assert md.shape == om.shape
+            both = (md > 0) & (om > 0)
+            assert ((md > 0) == (om > 0)).mean() > 0.995
+            assert (np.abs(md[both] - om[both]) < 1e-3).mean() > 0.999
+
+
+def test_lost_session_in_a_batch_leaves_the_others_alone(gpu):
+    a_case = helpers.make_case(width=160, height=120, dim=96, size=0.75, frames=3, seed=23)
+    b_case = helpers.make_case(width=320, height=240, dim=64, size=1.0, frames=3, seed=24)
+    with V.Session(a_case["cfg"]) as a:
+        for k in range(3):
+            a.scan_frame_host(a_case["depth"][k])
+        alone = a.pose()[1]
+        alone_w = a.volume()[1]
+    with V.Session(a_case["cfg"]) as a, V.Session(b_case["cfg"]) as b, V.Batch() as batch:
+        for k in range(3):
+            fb = b_case["depth"][k] if k != 1 else np.zeros_like(b_case["depth"][k])
+            T, tracked = batch.step_host([a, b], [a_case["depth"][k], fb])
+            if k == 1:
+                assert list(tracked) == [True, False]
+        assert np.array_equal(a.pose()[1], alone)
+        assert np.array_equal(a.volume()[1], alone_w)
+
+
+def test_largest_volume_and_image(gpu):
+    """1024^3 voxels (4 GiB of int16+uint16) and a 2048-pixel-wide image run;
+    one step more on either axis is refused"""
+    w, h = 2048, 1536
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=2, seed=25)
+    depth, gt, centre = V.synth_generate(sc)
+    origin, vox = V.cube_around(centre, 1.5, 1024)
+    cfg = V.default_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, dim=(1024, 1024, 1024), origin=origin,
+                           voxel_size=vox, mu=0.02)
+    with V.Session(cfg) as s:
+        for k in range(2):
+            T, tracked = s.scan_frame_host(depth[k])
+            assert tracked
+        assert helpers.camera_centre_err(T, gt[1]) < 5e-3
+        md = s.maps(0)["model_depth"]
+        assert (md > 0).mean() > 0.3
+    for bad in ((1032, 1024, 1024), (1024, 1024, 1032)):
+        cfg.dim[0], cfg.dim[1], cfg.dim[2] = bad
+        with pytest.raises(V.VsError) as e:
+            V.Session(cfg)
+        assert e.value.code == V.VS_ERR_ARG
+    wide = V.default_config(w + 8, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, dim=(64, 64, 64), origin=origin,
+                            voxel_size=vox * 16, mu=0.02)
+    with pytest.raises(V.VsError) as e:
+        V.Session(wide)
+    assert e.value.code == V.VS_ERR_ARG
