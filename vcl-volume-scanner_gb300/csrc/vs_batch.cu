@@ -9,13 +9,16 @@
 // before it reuses that step's buffers.  A step ends by gathering every
 // slot's pose head into one buffer that a single copy brings to the host.
 //
-// ICP runs as kIcpGroups independent launch sequences on branches of the
-// graph, each over a share of the sessions (split by pixel count).  Every ICP launch
-// ends with a tail in which only the blocks that close a session's iteration
-// (a reduction and an FP64 solve) still run; with several sequences in
-// flight the other sequences' blocks fill the SMs that the tail leaves idle.  A
-// session's sums do not depend on which sessions share its launch, so the
-// split changes no result.
+// The sessions are split into kIcpGroups groups (by pixel count), and each
+// group's whole frame (filter, maps, ICP, integration, ray-cast) runs as its
+// own launch sequence on a branch of the graph.  Every persistent launch ends
+// with a tail in which a few blocks still run (for ICP: the blocks closing a
+// session's iteration with a reduction and an FP64 solve; for the ray-cast:
+// the last tiles); with several sequences in flight the other sequences'
+// blocks fill the SMs that a tail leaves idle.  A session's work and sums do
+// not depend on which sessions share its launches, so the split changes no
+// result.  With stage timing on, the stages run one after another over the
+// whole batch (ICP still on branches) so that each stage's time is its own.
 //
 // The graph depends only on the schedule it was captured for: the deepest
 // pyramid and the largest ICP iteration count per level among the sessions,
@@ -57,7 +60,7 @@ constexpr int kRing = 2;
 #ifndef VS_ICP_GROUPS
 #define VS_ICP_GROUPS 2
 #endif
-constexpr int kIcpGroups = VS_ICP_GROUPS;  // concurrent ICP launch sequences
+constexpr int kIcpGroups = VS_ICP_GROUPS;  // concurrent per-frame launch sequences
 
 }  // namespace
 
@@ -91,6 +94,17 @@ void drop_graphs(vs_batch* b) {
     if (e) cudaGraphExecDestroy(e), e = nullptr;
 }
 
+// one group's per-frame chain on one stream
+void record_chain(vs_batch* b, const BatchTable* t, cudaStream_t st) {
+  const Schedule& k = b->sched;
+  launch_filter(t, st);
+  if (k.inmaps) launch_input_maps(t, st);
+  launch_icp(t, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
+  launch_integrate(t, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
+  launch_raycast(t, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr, nullptr,
+                 nullptr, st, b->shape, nullptr, k.color != 0);
+}
+
 void record_step(vs_batch* b, int r, cudaStream_t st) {
   const Schedule& k = b->sched;
   auto mark = [&](int i) {
@@ -98,24 +112,38 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
   };
   cudaMemcpyAsync(b->d_tab, b->h_tab[r], sizeof(BatchTable), cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(b->d_grp, b->h_grp[r], kIcpGroups * sizeof(BatchTable), cudaMemcpyHostToDevice, st);
-  mark(0);
-  launch_filter(b->d_tab, st);
-  if (k.inmaps) launch_input_maps(b->d_tab, st);
-  mark(1);
-  cudaEventRecord(b->fork, st);
-  for (int g = 1; g < kIcpGroups; g++) cudaStreamWaitEvent(b->side[g], b->fork, 0);
-  launch_icp(b->d_grp, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
-  for (int g = 1; g < kIcpGroups; g++) {
-    launch_icp(b->d_grp + g, k.levels, k.iters, k.reduce_mode, b->side[g], true, nullptr);
-    cudaEventRecord(b->join[g], b->side[g]);
-    cudaStreamWaitEvent(st, b->join[g], 0);
+  if (!k.timing) {
+    // every group's whole frame on its own branch
+    cudaEventRecord(b->fork, st);
+    for (int g = 1; g < kIcpGroups; g++) cudaStreamWaitEvent(b->side[g], b->fork, 0);
+    record_chain(b, b->d_grp, st);
+    for (int g = 1; g < kIcpGroups; g++) {
+      record_chain(b, b->d_grp + g, b->side[g]);
+      cudaEventRecord(b->join[g], b->side[g]);
+      cudaStreamWaitEvent(st, b->join[g], 0);
+    }
+  } else {
+    // stage timing: the stages one after another (ICP still on branches), so
+    // that each stage's time is its own
+    mark(0);
+    launch_filter(b->d_tab, st);
+    if (k.inmaps) launch_input_maps(b->d_tab, st);
+    mark(1);
+    cudaEventRecord(b->fork, st);
+    for (int g = 1; g < kIcpGroups; g++) cudaStreamWaitEvent(b->side[g], b->fork, 0);
+    launch_icp(b->d_grp, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
+    for (int g = 1; g < kIcpGroups; g++) {
+      launch_icp(b->d_grp + g, k.levels, k.iters, k.reduce_mode, b->side[g], true, nullptr);
+      cudaEventRecord(b->join[g], b->side[g]);
+      cudaStreamWaitEvent(st, b->join[g], 0);
+    }
+    mark(2);
+    launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
+    mark(3);
+    launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
+                   nullptr, nullptr, st, b->shape, nullptr, k.color != 0);
+    mark(4);
   }
-  mark(2);
-  launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
-  mark(3);
-  launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
-                 nullptr, nullptr, st, b->shape, nullptr, k.color != 0);
-  mark(4);
   launch_gather_heads(b->d_tab, b->d_heads, st);
   cudaMemcpyAsync(b->h_heads[r], b->d_heads, kMaxSlots * kPoseHeadBytes, cudaMemcpyDeviceToHost, st);
 }
