@@ -3,6 +3,9 @@
 * oracle/_build/liboracle.so  -- the C++ restatement (oracle.cpp), always.
 * oracle/_ref/libref_pin.so   -- the reference's own _yooji_math_inlines.h
   compiled from the reference tree, only where that tree is present.
+* oracle/_ref/libref_pin_cuda.so -- the reference's own _yooji_cuda_math.h
+  (per-pixel / per-voxel helpers) compiled as host C++ with the stand-ins of
+  oracle/ref_shim/, likewise only where the tree is present.
 
 No -march flags: the same source must build on x86-64 and aarch64.
 -ffp-contract=off keeps GCC from fusing multiply-adds (the CUDA side builds
@@ -49,7 +52,23 @@ def build_ref_pin(force=False):
     return out
 
 
+def build_ref_pin_cuda(force=False):
+    """Returns the path of libref_pin_cuda.so, or None when the reference tree is absent."""
+    if not os.path.isdir(REF_UTIL):
+        return None
+    out = os.path.join(HERE, "_ref", "libref_pin_cuda.so")
+    src = os.path.join(HERE, "ref_pin_cuda.cpp")
+    shim = os.path.join(HERE, "ref_shim")
+    deps = [src, os.path.join(shim, "ref_cuda_shim.h"), os.path.join(REF_UTIL, "_yooji_cuda_math.h"),
+            os.path.join(REF_UTIL, "_yooji_math_inlines.h")]
+    if force or not _newer(out, deps):
+        os.makedirs(os.path.dirname(out), exist_ok=True)
+        subprocess.check_call([CXX] + FLAGS + ["-fpermissive", "-w", "-I", shim, "-I", REF_UTIL, "-o", out, src])
+    return out
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref_pin(force))
+    print(build_ref_pin_cuda(force))

@@ -1619,6 +1619,38 @@ uint32_t or_update_valid_volume(or_volume* ov, const uint8_t* valid) {
       }
   return carved;
 }
+// single primitives of the restatement (float), for the reference pin
+void or_prim_cholesky6(const float* A, float* L) { cholesky<float>(A, L); }
+int or_prim_chol_solve6(const float* L, const float* b, float* x) { return chol_solve<float>(L, b, x) ? 1 : 0; }
+int or_prim_bilinear3(float xf, float yf, int w, int h, const float* map3, int normalise, float* out3) {
+  V3<float> o{0, 0, 0};
+  if (!bilinear3<float>(xf, yf, w, h, map3, o)) return 0;
+  if (normalise) o = normalised(o);
+  out3[0] = o.x, out3[1] = o.y, out3[2] = o.z;
+  return 1;
+}
+void or_prim_project(const float* p3, const float* K, float* uv) {
+  project<float>(v3<float>(p3[0], p3[1], p3[2]), K, uv[0], uv[1]);
+}
+void or_prim_back_project(float u, float v, const float* K, float d, float* p3) {
+  const V3<float> o = back_project<float>(u, v, K, d);
+  p3[0] = o.x, p3[1] = o.y, p3[2] = o.z;
+}
+void or_prim_transform(const float* p3, const float* T, int rotate_only, float* out3) {
+  const V3<float> p = v3<float>(p3[0], p3[1], p3[2]);
+  const V3<float> o = rotate_only ? rotate<float>(p, T) : transform<float>(p, T);
+  out3[0] = o.x, out3[1] = o.y, out3[2] = o.z;
+}
+int or_prim_pos_in_voxel(const float* p3, const float* origin, const int* dim, float vox_inv, float* out3) {
+  V3<float> o;
+  const bool ok = pos_in_voxel<float>(v3<float>(p3[0], p3[1], p3[2]), origin, dim, vox_inv, o);
+  out3[0] = o.x, out3[1] = o.y, out3[2] = o.z;
+  return ok ? 1 : 0;
+}
+void or_prim_pos_in_world(const float* v, const float* origin, float vox_inv, float* out3) {
+  const V3<float> o = pos_in_world<float>(v3<float>(v[0], v[1], v[2]), origin, vox_inv);
+  out3[0] = o.x, out3[1] = o.y, out3[2] = o.z;
+}
 uint64_t or_extract_mesh(const or_volume* v, float* xyz, uint8_t* rgb, uint64_t capacity) {
   return extract_mesh<float>(v->v, xyz, rgb, capacity);
 }

@@ -102,6 +102,19 @@ void or_render_variant(const or_volume* v, int level, int mode, const float* T_g
                        uint8_t* img, uint8_t* rgb);
 /* valid-volume carving over the last integration's sub-cube flags */
 uint32_t or_update_valid_volume(or_volume* v, const uint8_t* valid);
+/* single primitives of the restatement (float), pinned against the
+ * reference's own _yooji_cuda_math.h: 6x6 Cholesky factor and solve, the
+ * bilinear vertex / normal map lookups (normalise = 1: the normal form),
+ * projection, back-projection, transform (rotate_only = 1: rotation part),
+ * position in voxel / world coordinates */
+void or_prim_cholesky6(const float* A, float* L);
+int or_prim_chol_solve6(const float* L, const float* b, float* x);
+int or_prim_bilinear3(float xf, float yf, int w, int h, const float* map3, int normalise, float* out3);
+void or_prim_project(const float* p3, const float* K, float* uv);
+void or_prim_back_project(float u, float v, const float* K, float d, float* p3);
+void or_prim_transform(const float* p3, const float* T, int rotate_only, float* out3);
+int or_prim_pos_in_voxel(const float* p3, const float* origin, const int* dim, float vox_inv, float* out3);
+void or_prim_pos_in_world(const float* v, const float* origin, float vox_inv, float* out3);
 /* reference integration: sub-cube activation then TSDF update */
 void or_integrate(or_volume* v, const float* depth, const float* T_gc,
                   const float* T_cg);

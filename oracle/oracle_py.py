@@ -82,6 +82,14 @@ def load():
             "or_extract_mesh": (ctypes.c_uint64, [P, P, P, ctypes.c_uint64]),
             "or_render_variant": (None, [P, I, I, P, P, P, P, P, P, P, P, P]),
             "or_update_valid_volume": (ctypes.c_uint32, [P, P]),
+            "or_prim_cholesky6": (None, [P, P]),
+            "or_prim_chol_solve6": (I, [P, P, P]),
+            "or_prim_bilinear3": (I, [F, F, I, I, P, I, P]),
+            "or_prim_project": (None, [P, P, P]),
+            "or_prim_back_project": (None, [F, F, P, F, P]),
+            "or_prim_transform": (None, [P, P, I, P]),
+            "or_prim_pos_in_voxel": (I, [P, P, P, F, P]),
+            "or_prim_pos_in_world": (None, [P, P, F, P]),
             "or_warp_depth": (None, [P, I, I, P, P, P, I, I, P]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
@@ -115,6 +123,35 @@ def load_ref_pin():
         lib.ref_matmul4.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         _ref = lib
     return _ref
+
+
+_ref_cuda = None
+
+
+def load_ref_pin_cuda():
+    """The reference's own device math header compiled as host code (None when absent)."""
+    global _ref_cuda
+    if _ref_cuda is None:
+        import build_oracle as _b
+        path = _b.build_ref_pin_cuda()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        sig = {
+            "ref_lld6": (I, [P, P]), "ref_sls6": (I, [P, P, P]),
+            "ref_giv": (I, [F, F, I, I, P, P]), "ref_gin": (I, [F, F, I, I, P, P]),
+            "ref_project": (None, [P, P, P]), "ref_back_project": (None, [F, F, P, F, P]),
+            "ref_transform": (None, [P, P, P]), "ref_rotate": (None, [P, P, P]),
+            "ref_camera_center": (None, [P, P]),
+            "ref_pos_in_voxel": (I, [P, P, P, F, P]), "ref_pos_in_world": (None, [P, P, P, F, P]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(lib, name)
+            f.restype = res
+            f.argtypes = args
+        _ref_cuda = lib
+    return _ref_cuda
 
 
 def config_from_vs(vs_cfg, reduce_mode=None, tsdf_store=None):

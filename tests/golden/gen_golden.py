@@ -7,6 +7,15 @@ refpin.npz
     d_im_Inverse_Matrix_4x4, d_mmm_Multiply_Matrix_Matrix), compiled from the
     reference tree by oracle/build_oracle.py.  These pin the oracle's pose
     algebra bit for bit.
+refpin_cuda.npz
+    Inputs and outputs of the reference's own STAC/Util/_yooji_cuda_math.h
+    helpers, compiled as host C++ (oracle/ref_pin_cuda.cpp with the stand-ins
+    of oracle/ref_shim/): 6x6 Cholesky factors and solves
+    (d_lld_LL_Decomposition, d_sls_Solve_Linear_System_using_LLD, including
+    singular and negative-pivot systems), bilinear vertex / normal lookups
+    (d_giv / d_gin, with -100 sentinels and integer coordinates), projection,
+    back-projection, transform, rotation, camera centre and voxel / world
+    positions.  These pin the oracle's restatements of them bit for bit.
 seq_small.npz
     A 6-frame 160x120 synthetic sequence (uint16 input frames stored, so no
     cross-host generator identity is assumed) and the oracle's outputs for it
@@ -77,7 +86,83 @@ def seq_small():
                         gt=case["gt"])
 
 
+def refpin_cuda():
+    ref = O.load_ref_pin_cuda()
+    if ref is None:
+        raise SystemExit("the reference tree is not mounted; refpin_cuda.npz cannot be regenerated")
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    rng = np.random.default_rng(20240602)
+    # 6x6 systems: well and badly conditioned, singular, a negative pivot
+    n = 48
+    A = np.empty((n, 36), np.float32)
+    for i in range(n):
+        M = rng.standard_normal((6, 6)).astype(np.float32) * np.float32(10.0 ** (i % 7 - 3))
+        a = (M @ M.T).astype(np.float32)
+        if i % 8 == 6:
+            a[3, :] = 0.0
+            a[:, 3] = 0.0
+        if i % 8 == 7:
+            a[2, 2] = -1.0
+        A[i] = a.reshape(36)
+    rhs = rng.standard_normal((n, 6)).astype(np.float32)
+    L = np.zeros((n, 36), np.float32)
+    x = np.zeros((n, 6), np.float32)
+    ok = np.zeros(n, np.int32)
+    for i in range(n):
+        ref.ref_lld6(p(A[i]), p(L[i]))
+        ok[i] = ref.ref_sls6(p(L[i]), p(rhs[i]), p(x[i]))
+    # bilinear lookups on one 13x9 map with sentinels
+    w, h = 13, 9
+    mp = rng.standard_normal((h, w, 3)).astype(np.float32)
+    mp[rng.random((h, w)) < 0.12] = -100.0
+    mp = np.ascontiguousarray(mp.reshape(-1))
+    m = 400
+    xy = np.stack([rng.uniform(-0.5, w - 0.5, m), rng.uniform(-0.5, h - 0.5, m)], 1).astype(np.float32)
+    xy[::4, 0] = np.floor(xy[::4, 0])
+    xy[1::4, 1] = np.floor(xy[1::4, 1])
+    giv = np.zeros((m, 3), np.float32)
+    gin = np.zeros((m, 3), np.float32)
+    giv_ok = np.zeros(m, np.int32)
+    gin_ok = np.zeros(m, np.int32)
+    for i in range(m):
+        giv_ok[i] = ref.ref_giv(float(xy[i, 0]), float(xy[i, 1]), w, h, p(mp), p(giv[i]))
+        gin_ok[i] = ref.ref_gin(float(xy[i, 0]), float(xy[i, 1]), w, h, p(mp), p(gin[i]))
+    # geometry
+    g = 200
+    K = np.stack([rng.uniform(100, 600, g), rng.uniform(100, 600, g), rng.uniform(100, 400, g),
+                  rng.uniform(80, 300, g)], 1).astype(np.float32)
+    p3 = (rng.standard_normal((g, 3)) * [0.5, 0.5, 0.3] + [0, 0, 1.2]).astype(np.float32)
+    T = rng.standard_normal((g, 16)).astype(np.float32)
+    uvd = np.stack([rng.uniform(0, 640, g), rng.uniform(0, 480, g), rng.uniform(0.3, 3, g)], 1).astype(np.float32)
+    org = rng.uniform(-1, 0, (g, 3)).astype(np.float32)
+    dim = np.array([128, 96, 64], np.int32)
+    inv = rng.uniform(50, 500, g).astype(np.float32)
+    q = (org + rng.uniform(-0.1, 1.2, (g, 3))).astype(np.float32)
+    vox = rng.uniform(-1, 130, (g, 3)).astype(np.float32)
+    proj = np.zeros((g, 2), np.float32)
+    bproj = np.zeros((g, 3), np.float32)
+    trans = np.zeros((g, 3), np.float32)
+    rot = np.zeros((g, 3), np.float32)
+    cen = np.zeros((g, 3), np.float32)
+    gpv = np.zeros((g, 3), np.float32)
+    gpv_ok = np.zeros(g, np.int32)
+    gpw = np.zeros((g, 3), np.float32)
+    for i in range(g):
+        ref.ref_project(p(p3[i]), p(K[i]), p(proj[i]))
+        ref.ref_back_project(float(uvd[i, 0]), float(uvd[i, 1]), p(K[i]), float(uvd[i, 2]), p(bproj[i]))
+        ref.ref_transform(p(p3[i]), p(T[i]), p(trans[i]))
+        ref.ref_rotate(p(p3[i]), p(T[i]), p(rot[i]))
+        ref.ref_camera_center(p(T[i]), p(cen[i]))
+        gpv_ok[i] = ref.ref_pos_in_voxel(p(q[i]), p(org[i]), p(dim), float(inv[i]), p(gpv[i]))
+        ref.ref_pos_in_world(p(vox[i]), p(org[i]), p(dim), float(inv[i]), p(gpw[i]))
+    np.savez_compressed(os.path.join(OUT, "refpin_cuda.npz"), A=A, rhs=rhs, L=L, x=x, ok=ok, w=w, h=h, map=mp, xy=xy,
+                        giv=giv, gin=gin, giv_ok=giv_ok, gin_ok=gin_ok, K=K, p3=p3, T=T, uvd=uvd, org=org, dim=dim,
+                        inv=inv, q=q, vox=vox, proj=proj, bproj=bproj, trans=trans, rot=rot, cen=cen, gpv=gpv,
+                        gpv_ok=gpv_ok, gpw=gpw)
+
+
 if __name__ == "__main__":
     refpin()
+    refpin_cuda()
     seq_small()
     print("fixtures written to", OUT)
