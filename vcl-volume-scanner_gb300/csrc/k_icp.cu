@@ -94,11 +94,11 @@ __device__ inline bool icp_term(int x, int y, int w, int h, const float* K, cons
   Taps t;
   if (!tap_setup(u, v, w, h, t)) return false;
   const float4 va = __ldg(mvtx + t.i00), vb = __ldg(mvtx + t.i01), vc = __ldg(mvtx + t.i10), vd = __ldg(mvtx + t.i11);
-  const float4 na = __ldg(mnrm + t.i00), nb = __ldg(mnrm + t.i01), nc = __ldg(mnrm + t.i10), nd = __ldg(mnrm + t.i11);
   F3 p0;
   if (!interp(t, va, vb, vc, vd, p0)) return false;
   float dd = (p0.x - p1.x) * (p0.x - p1.x) + (p0.y - p1.y) * (p0.y - p1.y) + (p0.z - p1.z) * (p0.z - p1.z);
   if (dd > th_icp) return false;
+  const float4 na = __ldg(mnrm + t.i00), nb = __ldg(mnrm + t.i01), nc = __ldg(mnrm + t.i10), nd = __ldg(mnrm + t.i11);
   F3 n;
   if (!interp(t, na, nb, nc, nd, n)) return false;
   n = normalised(n);
@@ -492,8 +492,12 @@ __device__ __noinline__ void icp_solve_update(Pose* P, const double* fin, int le
 // (reduction + solve, ~10 us) simply takes no new range meanwhile, so the
 // closing work of different sessions overlaps instead of queueing behind a
 // static assignment.  The last block to leave clears the counters.
+#ifndef VS_ICP_MIN_BLOCKS
+#define VS_ICP_MIN_BLOCKS 3  // resident 256-thread blocks per SM the register allocation must allow
+#endif
+
 template <int MODE>
-__global__ void __launch_bounds__(kThreads, 3)
+__global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
     k_icp_iter(const BatchTable* __restrict__ bt, unsigned* __restrict__ work, int level, int iter) {
   typedef typename PartT<MODE>::type PT;
   __shared__ PT wsum[kThreads / 32][29];
@@ -685,7 +689,7 @@ void launch_icp(const BatchTable* bt, int max_levels, const int* max_iters, int 
   // tp_Track_Pose calls always track
   const bool with_init = init_T12 != nullptr;
   k_icp_begin<<<1, kMaxSlots, 0, st>>>(bt, frame_mode ? 1 : 0, with_init ? 1 : 0, init_T12);
-  const int grid = sm_count() * 3 < kIcpMaxBlocks ? sm_count() * 3 : kIcpMaxBlocks;  // 3 resident per SM
+  const int grid = sm_count() * VS_ICP_MIN_BLOCKS;  // every block resident
   unsigned* work = const_cast<unsigned*>(bt->work) + 2;
   for (int l = max_levels - 1; l >= 0; l--) {
     for (int i = 0; i < max_iters[l]; i++) {
