@@ -78,14 +78,10 @@ __device__ inline bool interp(const Taps& t, float4 a, float4 b, float4 c, float
 
 // d_cssfp_Compute_Single_Summand_with_Forward_Params.  Two rounds of reads:
 // the pixel's depth (and input normal), then the eight model-map taps.
-__device__ inline bool icp_term(int x, int y, int w, int h, const float* K, const float* __restrict__ depth,
-                                const float4* __restrict__ mvtx, const float4* __restrict__ mnrm,
-                                const float4* __restrict__ innrm, const float* T21, float th_icp,
-                                float cos_normal, float A[6], float& b) {
-  const float d1 = __ldg(depth + (size_t)y * w + x);
+__device__ inline bool icp_term(int x, int y, int w, int h, const float* K, float d1, float4 q,
+                                const float4* __restrict__ mvtx, const float4* __restrict__ mnrm, const float* T21,
+                                float th_icp, float cos_normal, float A[6], float& b) {
   const bool ntest = cos_normal > -2.0f;
-  float4 q = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-  if (ntest) q = __ldg(innrm + (size_t)y * w + x);
   if (d1 < 1.0e-6f) return false;
   F3 tp = back_project((float)x, (float)y, K, d1);
   F3 p1 = transform(tp, T21);
@@ -541,10 +537,28 @@ __global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
     Acc<MODE> acc;
     acc.zero();
     const int npix = w * h;
-    for (int p = vb * kThreads + threadIdx.x; p < npix; p += nvb * kThreads) {
-      int y = p / w, x = p - y * w;
+    const int stride = nvb * kThreads;
+    const bool ntest = cosn > -2.0f;
+    // the first-round reads (depth, input normal) of a thread's next pixel are
+    // in flight while its current pixel's taps are read
+    int p = vb * kThreads + threadIdx.x;
+    float d_next = 0.0f;
+    float4 q_next = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    if (p < npix) {
+      d_next = __ldg(depth + p);
+      if (ntest) q_next = __ldg(innrm + p);
+    }
+    while (p < npix) {
+      const float d1 = d_next;
+      const float4 qn = q_next;
+      const int y = p / w, x = p - y * w;
+      p += stride;
+      if (p < npix) {
+        d_next = __ldg(depth + p);
+        if (ntest) q_next = __ldg(innrm + p);
+      }
       float A[6], b;
-      if (!icp_term(x, y, w, h, K, depth, mvtx, mnrm, innrm, T21, th, cosn, A, b)) continue;
+      if (!icp_term(x, y, w, h, K, d1, qn, mvtx, mnrm, T21, th, cosn, A, b)) continue;
 #pragma unroll
       for (int i = 0; i < 6; i++)
 #pragma unroll
