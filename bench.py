@@ -194,7 +194,9 @@ class ClockSampler:
     def __init__(self, gpu_index):
         self.idx = gpu_index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % gpu_index)
+        # raw samples; the summary goes into the JSON line
+        self.path = os.path.join(os.environ.get("VS_BENCH_CLOCKS_DIR", os.path.join(ROOT, "_bench")),
+                                 "clocks_bench_%d.csv" % gpu_index)
 
     def start(self):
         try:
