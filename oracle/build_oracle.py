@@ -6,6 +6,9 @@
 * oracle/_ref/libref_pin_cuda.so -- the reference's own _yooji_cuda_math.h
   (per-pixel / per-voxel helpers) compiled as host C++ with the stand-ins of
   oracle/ref_shim/, likewise only where the tree is present.
+* oracle/_ref/libref_pin_render.so, libref_pin_integ.so -- the reference's own
+  renderer and integrator sources run as host code (see build_ref_pin_gpu),
+  likewise only where the tree is present.
 
 No -march flags: the same source must build on x86-64 and aarch64.
 -ffp-contract=off keeps GCC from fusing multiply-adds (the CUDA side builds
@@ -67,8 +70,70 @@ def build_ref_pin_cuda(force=False):
     return out
 
 
+REF_STAC = os.path.dirname(REF_UTIL)
+# kernel launches `k<<<grid, block>>>(` -> the host launch loop of the shim
+_LAUNCH = r"(\w+)\s*<<<([^<>]*)>>>\s*\("
+_GPU_SOURCES = {"math": "Util/z_yooji_cuda_math.cu", "renderer": "Engine/GPU/z_yooji_cuda_tsdf_renderer.cu",
+                "integrator": "Engine/GPU/z_yooji_cuda_volume_integrator.cu",
+                "tracker": "Engine/GPU/z_yooji_cuda_pose_tracker.cu"}
+
+
+def build_ref_pin_gpu(force=False):
+    """The reference's renderer and integrator run as host code.  Returns
+    {"render": path, "integ": path, "track": path}, or None when the reference tree is absent.
+
+    The launch syntax is the only text changed: each source is read from the
+    reference tree, its `<<<...>>>` launches are turned into calls of the host
+    launch loop, and the result is written to oracle/_ref/gen/ (a build
+    product, never committed) and compiled with oracle/ref_pin_gpu.cpp."""
+    import re
+    if not os.path.isdir(REF_STAC):
+        return None
+    gen = os.path.join(HERE, "_ref", "gen")
+    shim = os.path.join(HERE, "ref_shim", "gpu")
+    outs = {"render": os.path.join(HERE, "_ref", "libref_pin_render.so"),
+            "integ": os.path.join(HERE, "_ref", "libref_pin_integ.so"),
+            "track": os.path.join(HERE, "_ref", "libref_pin_track.so")}
+    srcs = [os.path.join(REF_STAC, v) for v in _GPU_SOURCES.values()]
+    deps = srcs + [os.path.join(HERE, f) for f in ("ref_pin_gpu.cpp", "ref_gpu_runtime.cpp")] + \
+        [os.path.join(shim, f) for f in os.listdir(shim)]
+    if not force and all(_newer(o, deps) for o in outs.values()):
+        return outs
+    os.makedirs(gen, exist_ok=True)
+    pat = re.compile(_LAUNCH)
+    for name, rel in _GPU_SOURCES.items():
+        with open(os.path.join(REF_STAC, rel), encoding="latin-1") as f:
+            text = f.read()
+        text = pat.sub(lambda m: "vs_launch_any(%s, [&](auto&&... vs_a) { %s(vs_a...); })(" % (m.group(2), m.group(1)),
+                       text)
+        with open(os.path.join(gen, name + ".cu.cpp"), "w", encoding="latin-1") as f:
+            f.write(text)
+        with open(os.path.join(gen, "tu_" + name + ".cpp"), "w") as f:
+            f.write('#include "ref_gpu_shim.h"\n#include "%s.cu.cpp"\n' % name)
+    inc = ["-I", shim, "-I", os.path.join(REF_STAC, "Engine", "GPU"), "-I", REF_UTIL, "-I", gen]
+    cflags = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-fpermissive", "-w"]
+    objs = {}
+    for name in ("math",):
+        objs[name] = os.path.join(gen, name + ".o")
+        subprocess.check_call([CXX] + cflags + inc + ["-c", "-x", "c++", os.path.join(gen, "tu_" + name + ".cpp"),
+                               "-o", objs[name]])
+    objs["rt"] = os.path.join(gen, "rt.o")
+    subprocess.check_call([CXX] + cflags + ["-I", shim, "-c", os.path.join(HERE, "ref_gpu_runtime.cpp"), "-o", objs["rt"]])
+    for key, macro in (("render", "REF_PIN_RENDER"), ("integ", "REF_PIN_INTEG"), ("track", "REF_PIN_TRACK")):
+        o = os.path.join(gen, key + ".o")
+        subprocess.check_call([CXX] + cflags + inc + ["-D" + macro, "-c", "-x", "c++",
+                               os.path.join(HERE, "ref_pin_gpu.cpp"), "-o", o])
+        subprocess.check_call([CXX, "-shared", "-o", outs[key], o, objs["math"], objs["rt"]])
+    # the rewritten sources and objects are intermediate: keep only the libraries
+    for f in os.listdir(gen):
+        os.remove(os.path.join(gen, f))
+    os.rmdir(gen)
+    return outs
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref_pin(force))
     print(build_ref_pin_cuda(force))
+    print(build_ref_pin_gpu(force))

@@ -1619,6 +1619,13 @@ uint32_t or_update_valid_volume(or_volume* ov, const uint8_t* valid) {
       }
   return carved;
 }
+// the expanded cube geometry of a configuration: centre[3], r_cube, 1/voxel
+void or_config_geometry(const or_config* cfg, float* out5) {
+  const Cfg<float> g = expand<float>(cfg);
+  for (int k = 0; k < 3; k++) out5[k] = g.center[k];
+  out5[3] = g.r_cube;
+  out5[4] = g.vox_inv;
+}
 // single primitives of the restatement (float), for the reference pin
 void or_prim_cholesky6(const float* A, float* L) { cholesky<float>(A, L); }
 int or_prim_chol_solve6(const float* L, const float* b, float* x) { return chol_solve<float>(L, b, x) ? 1 : 0; }
@@ -1646,6 +1653,14 @@ int or_prim_pos_in_voxel(const float* p3, const float* origin, const int* dim, f
   const bool ok = pos_in_voxel<float>(v3<float>(p3[0], p3[1], p3[2]), origin, dim, vox_inv, o);
   out3[0] = o.x, out3[1] = o.y, out3[2] = o.z;
   return ok ? 1 : 0;
+}
+int or_prim_icp_term(int x, int y, int w, int h, const float* K, const float* depth, const float* mvtx,
+                     const float* mnrm, const float* T21, float th_icp, float* A6, float* b) {
+  float A[6], bb = 0;
+  if (!icp_term<float>(x, y, w, h, K, depth, mvtx, mnrm, nullptr, T21, th_icp, -3.0f, A, bb)) return 0;
+  for (int i = 0; i < 6; i++) A6[i] = A[i];
+  *b = bb;
+  return 1;
 }
 void or_prim_pos_in_world(const float* v, const float* origin, float vox_inv, float* out3) {
   const V3<float> o = pos_in_world<float>(v3<float>(v[0], v[1], v[2]), origin, vox_inv);

@@ -102,6 +102,8 @@ void or_render_variant(const or_volume* v, int level, int mode, const float* T_g
                        uint8_t* img, uint8_t* rgb);
 /* valid-volume carving over the last integration's sub-cube flags */
 uint32_t or_update_valid_volume(or_volume* v, const uint8_t* valid);
+/* the expanded cube geometry: centre[3], r_cube, 1/voxel size */
+void or_config_geometry(const or_config* cfg, float* out5);
 /* single primitives of the restatement (float), pinned against the
  * reference's own _yooji_cuda_math.h: 6x6 Cholesky factor and solve, the
  * bilinear vertex / normal map lookups (normalise = 1: the normal form),
@@ -115,6 +117,10 @@ void or_prim_back_project(float u, float v, const float* K, float d, float* p3);
 void or_prim_transform(const float* p3, const float* T, int rotate_only, float* out3);
 int or_prim_pos_in_voxel(const float* p3, const float* origin, const int* dim, float vox_inv, float* out3);
 void or_prim_pos_in_world(const float* v, const float* origin, float vox_inv, float* out3);
+/* one pixel's ICP term at a pyramid level (no input-normal test): A (6) and b;
+ * returns 0 where the pixel gives no term */
+int or_prim_icp_term(int x, int y, int w, int h, const float* K, const float* depth, const float* mvtx,
+                     const float* mnrm, const float* T21, float th_icp, float* A6, float* b);
 /* reference integration: sub-cube activation then TSDF update */
 void or_integrate(or_volume* v, const float* depth, const float* T_gc,
                   const float* T_cg);

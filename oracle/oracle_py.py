@@ -82,6 +82,7 @@ def load():
             "or_extract_mesh": (ctypes.c_uint64, [P, P, P, ctypes.c_uint64]),
             "or_render_variant": (None, [P, I, I, P, P, P, P, P, P, P, P, P]),
             "or_update_valid_volume": (ctypes.c_uint32, [P, P]),
+            "or_config_geometry": (None, [P, P]),
             "or_prim_cholesky6": (None, [P, P]),
             "or_prim_chol_solve6": (I, [P, P, P]),
             "or_prim_bilinear3": (I, [F, F, I, I, P, I, P]),
@@ -90,6 +91,7 @@ def load():
             "or_prim_transform": (None, [P, P, I, P]),
             "or_prim_pos_in_voxel": (I, [P, P, P, F, P]),
             "or_prim_pos_in_world": (None, [P, P, F, P]),
+            "or_prim_icp_term": (I, [I, I, I, I, P, P, P, P, P, F, P, P]),
             "or_warp_depth": (None, [P, I, I, P, P, P, I, I, P]),
             "or_session_create": (P, [P]),
             "or_session_create_f64": (P, [P]),
@@ -152,6 +154,30 @@ def load_ref_pin_cuda():
             f.argtypes = args
         _ref_cuda = lib
     return _ref_cuda
+
+
+_ref_gpu = None
+
+
+def load_ref_pin_gpu():
+    """The reference's renderer, integrator and tracker run as host code:
+    (render, integ, track) libraries, or None when the reference tree is absent."""
+    global _ref_gpu
+    if _ref_gpu is None:
+        import build_oracle as _b
+        paths = _b.build_ref_pin_gpu()
+        if paths is None:
+            return None
+        r, i, t = (ctypes.CDLL(paths[k]) for k in ("render", "integ", "track"))
+        P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        r.ref_render_icp.restype = I
+        r.ref_render_icp.argtypes = [I, I, P, I, P, P, P, F, F, F, P, P, P, P, P, P, P, P, P, P]
+        i.ref_integrate_color.restype = I
+        i.ref_integrate_color.argtypes = [I, I, P, P, P, P, F, F, F, P, P, P, P, P, P, P]
+        t.ref_icp_terms.restype = None
+        t.ref_icp_terms.argtypes = [I, I, P, P, P, P, P, P, F, P, P, P]
+        _ref_gpu = (r, i, t)
+    return _ref_gpu
 
 
 def config_from_vs(vs_cfg, reduce_mode=None, tsdf_store=None):

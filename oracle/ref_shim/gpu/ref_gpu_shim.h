@@ -1,0 +1,131 @@
+// Host stand-ins for the CUDA runtime, curand and InfiniTAM's ITMMath, so that
+// the reference's GPU sources (STAC/Engine/GPU/*.cu) compile as plain host C++
+// for the reference-pin harness oracle/ref_pin_gpu.cpp (TEST INFRASTRUCTURE
+// ONLY; nothing here runs on a GPU).  The harness calls the reference's
+// __device__ functions directly and runs its kernels as host loops over the
+// launch grid (threadIdx / blockIdx below are the loop's variables).
+//
+// Arithmetic: the functions below are restatements, kept to what the pinned
+// code uses.  __float2int_rn rounds half to even (as the CUDA intrinsic is
+// documented); ITMMath's vectors are plain structs whose operators work
+// component by component in the order ITMMath writes them.
+#pragma once
+#include <cmath>
+#include <cstddef>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <cstdint>
+
+#define __device__
+#define __host__
+#define __global__
+#define __constant__
+#define __shared__ static
+#define __forceinline__ inline
+#define __align__(n)
+
+using std::abs;
+using std::sqrt;
+typedef unsigned char uchar;
+typedef unsigned short ushort;
+typedef unsigned int uint;
+
+struct dim3 {
+  unsigned x = 1, y = 1, z = 1;
+  dim3(unsigned a = 1, unsigned b = 1, unsigned c = 1) : x(a), y(b), z(c) {}
+};
+struct uint3_ {
+  unsigned x = 0, y = 0, z = 0;
+};
+// the launch emulation sets these before each call of a kernel body
+extern uint3_ threadIdx, blockIdx;
+extern dim3 blockDim, gridDim;
+struct int2 {
+  int x, y;
+};
+struct int3 {
+  int x, y, z;
+};
+struct float2 {
+  float x, y;
+};
+struct float3 {
+  float x, y, z;
+};
+struct float4 {
+  float x, y, z, w;
+};
+inline void __syncthreads() {}
+inline int __float2int_rn(float x) { return (int)std::nearbyint(x); }  // default rounding mode: half to even
+// IEEE round-to-nearest operations by their definition
+inline float __fadd_rn(float a, float b) { return a + b; }
+inline float __fmul_rn(float a, float b) { return a * b; }
+inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
+inline float __int2float_rn(int x) { return (float)x; }
+
+// _yooji_cuda_math.hpp:98 (GKvMatrix<T>::to_host) names an undeclared
+// `out_vol`; MSVC never checks the uninstantiated template, GCC needs the name
+// to exist.  Nothing here instantiates it.
+static void* out_vol;
+
+// The runtime on host memory: "device" buffers are host buffers, copies are
+// memcpy, a symbol is the plain global of the same name.
+typedef int cudaError_t;
+typedef struct CUstream_st* cudaStream_t;
+enum cudaMemcpyKind { cudaMemcpyHostToHost, cudaMemcpyHostToDevice, cudaMemcpyDeviceToHost, cudaMemcpyDeviceToDevice };
+struct cudaChannelFormatDesc {
+  int x, y, z, w, f;
+};
+cudaError_t cudaMalloc(void**, size_t);
+cudaError_t cudaFree(void*);
+cudaError_t cudaMemcpy(void*, const void*, size_t, cudaMemcpyKind);
+cudaError_t cudaMemset(void*, int, size_t);
+cudaError_t cudaDeviceSynchronize();
+cudaError_t cudaGetLastError();
+const char* cudaGetErrorString(cudaError_t);
+template <class T>
+cudaError_t cudaMemcpyToSymbol(T& sym, const void* src, size_t n, size_t off = 0,
+                               cudaMemcpyKind = cudaMemcpyHostToDevice) {
+  std::memcpy(reinterpret_cast<char*>(&sym) + off, src, n);
+  return 0;
+}
+template <class T>
+cudaError_t cudaMemcpyFromSymbol(void* dst, const T& sym, size_t n, size_t off = 0,
+                                 cudaMemcpyKind = cudaMemcpyDeviceToHost) {
+  std::memcpy(dst, reinterpret_cast<const char*>(&sym) + off, n);
+  return 0;
+}
+#define checkCudaErrors(x) (x)
+
+// a kernel launch `k<<<grid, block>>>(args)` becomes
+// `vs_launch(grid, block, [&](auto&&... a) { k(a...); })(args)`: every thread
+// of the grid runs the kernel body in turn (the kernels pinned here have no
+// shared memory and no barriers, so the order is immaterial)
+template <class F>
+struct VsLaunch {
+  dim3 g, b;
+  F f;
+  template <class... A>
+  void operator()(A&&... a) {
+    gridDim = g;
+    blockDim = b;
+    for (unsigned bz = 0; bz < g.z; bz++)
+      for (unsigned by = 0; by < g.y; by++)
+        for (unsigned bx = 0; bx < g.x; bx++)
+          for (unsigned tz = 0; tz < b.z; tz++)
+            for (unsigned ty = 0; ty < b.y; ty++)
+              for (unsigned tx = 0; tx < b.x; tx++) {
+                blockIdx.x = bx, blockIdx.y = by, blockIdx.z = bz;
+                threadIdx.x = tx, threadIdx.y = ty, threadIdx.z = tz;
+                f(a...);
+              }
+  }
+};
+template <class F>
+VsLaunch<F> vs_launch(dim3 g, dim3 b, F f) {
+  return VsLaunch<F>{g, b, f};
+}
+inline dim3 vs_dim3(dim3 d) { return d; }
+inline dim3 vs_dim3(int n) { return dim3((unsigned)n); }
+#define vs_launch_any(g, b, f) vs_launch(vs_dim3(g), vs_dim3(b), f)

@@ -16,6 +16,14 @@ refpin_cuda.npz
     (d_giv / d_gin, with -100 sentinels and integer coordinates), projection,
     back-projection, transform, rotation, camera centre and voxel / world
     positions.  These pin the oracle's restatements of them bit for bit.
+refpin_gpu.npz
+    Two frames (80x60 depth with a zero border and a colour image with no zero
+    texel, so every colour sample interpolates) integrated into a 48^3 cube,
+    and the ray-cast maps of every pyramid level from a third pose, computed
+    by the reference's own renderer and integrator sources run as host code
+    (oracle/ref_pin_gpu.cpp): float TSDF, uchar weights and colour after each
+    frame, depth / vertex / normal / shading per level.  These pin the
+    oracle's integration and ray-cast bit for bit.
 seq_small.npz
     A 6-frame 160x120 synthetic sequence (uint16 input frames stored, so no
     cross-host generator identity is assumed) and the oracle's outputs for it
@@ -161,8 +169,104 @@ def refpin_cuda():
                         gpv_ok=gpv_ok, gpw=gpw)
 
 
+def refpin_gpu():
+    libs = O.load_ref_pin_gpu()
+    if libs is None:
+        raise SystemExit("the reference tree is not mounted; refpin_gpu.npz cannot be regenerated")
+    rr, ri, rt = libs
+    import vs_scanner as V
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    w, h, dim, size = 80, 60, 48, 0.75
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=3, seed=9, dropout_iid=0.01)
+    depth_mm, rgb, gt, centre = V.synth_generate_rgb(sc)
+    origin, vox = V.cube_around(centre, size, dim)
+    cfg = dict(width=w, height=h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, dim=dim, origin=np.array(origin, np.float32),
+               voxel_size=vox, mu=0.03, max_w=100.0)
+    oc = refpin_gpu_config(cfg)
+    geo = np.zeros(5, np.float32)
+    O.load().or_config_geometry(ctypes.byref(oc), p(geo))
+    K0 = np.array([oc.fx, oc.fy, oc.cx, oc.cy], np.float32)
+    dims = np.array([dim] * 3, np.int32)
+    org = np.array(list(oc.origin), np.float32)
+    cen = np.ascontiguousarray(geo[:3])
+    n = dim ** 3
+    t = np.ones(n, np.float32)
+    wt = np.zeros(n, np.uint8)
+    col = np.zeros(3 * n, np.uint8)
+    depths, imgs, tsdf, weight, colour = [], [], [], [], []
+    for k in range(2):
+        raw = O.depth_to_m(depth_mm[k]).astype(np.float32)
+        raw[0, :] = raw[-1, :] = raw[:, 0] = raw[:, -1] = 0.0
+        img = np.ascontiguousarray(np.maximum(rgb[k], 1), np.uint8)
+        Tgc = np.ascontiguousarray(gt[k], np.float32)
+        Tcg = O.pose_inverse(Tgc)
+        ri.ref_integrate_color(w, h, p(K0), p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(t), p(wt),
+                               p(col), p(np.ascontiguousarray(raw)), p(img), p(Tgc), p(np.ascontiguousarray(Tcg)))
+        depths.append(raw)
+        imgs.append(img)
+        tsdf.append(t.copy())
+        weight.append(wt.copy())
+        colour.append(col.copy())
+    Tgc = np.ascontiguousarray(gt[2], np.float32)
+    Tcg = np.ascontiguousarray(O.pose_inverse(Tgc))
+    cam = np.ascontiguousarray(O.camera_center(Tgc), np.float32)
+    light = np.array([0, 0, -1], np.float32)
+    maps = {}
+    for l in range(3):
+        lw, lh = w >> l, h >> l
+        d, v, nn, im = (np.zeros(lw * lh, np.float32), np.zeros(3 * lw * lh, np.float32),
+                        np.zeros(3 * lw * lh, np.float32), np.zeros(lw * lh, np.uint8))
+        rr.ref_render_icp(w, h, p(K0), l, p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(t), p(wt),
+                          p(Tgc), p(Tcg), p(cam), p(light), p(d), p(v), p(nn), p(im))
+        maps.update({"depth%d" % l: d, "vertex%d" % l: v, "normal%d" % l: nn, "img%d" % l: im})
+    # the per-pixel ICP term against the level-1 model maps: the next frame's
+    # depth, subsampled, and an increment a little off the identity
+    icp = icp_case(np.ascontiguousarray(O.depth_to_m(depth_mm[2])[::2, ::2], np.float32))
+    K1 = np.array([oc.fx / 2, oc.fy / 2, oc.cx / 2, oc.cy / 2], np.float32)
+    n1 = (w >> 1) * (h >> 1)
+    ATA, ATb, ok = np.zeros((n1, 36), np.float32), np.zeros((n1, 6), np.float32), np.zeros(n1, np.uint8)
+    rt.ref_icp_terms(w >> 1, h >> 1, p(K1), p(icp["depth"]), p(maps["depth1"]), p(maps["vertex1"]), p(maps["normal1"]),
+                     p(icp["T21"]), 0.01, p(ATA), p(ATb), p(ok))
+    maps.update({"icp_depth": icp["depth"], "icp_T21": icp["T21"], "icp_K": K1, "icp_ATA": ATA, "icp_ATb": ATb,
+                 "icp_ok": ok})
+    np.savez_compressed(os.path.join(OUT, "refpin_gpu.npz"), cfg_w=w, cfg_h=h, cfg_f=f, cfg_dim=dim,
+                        cfg_origin=cfg["origin"], cfg_vox=vox, cfg_mu=0.03, cfg_maxw=100.0, depth=np.stack(depths),
+                        rgb=np.stack(imgs), T=np.ascontiguousarray(gt[:3], np.float32), tsdf=np.stack(tsdf),
+                        weight=np.stack(weight), colour=np.stack(colour), **maps)
+
+
+def icp_case(depth):
+    """a depth frame and an increment T21 (4x4 row-major float32): a rotation
+    of 0.6 degrees about (1, 2, 3) / |.| and a 4 mm shift"""
+    a = np.array([1.0, 2.0, 3.0]) / np.sqrt(14.0)
+    th = np.deg2rad(0.6)
+    Kx = np.array([[0, -a[2], a[1]], [a[2], 0, -a[0]], [-a[1], a[0], 0]])
+    R = np.eye(3) + np.sin(th) * Kx + (1 - np.cos(th)) * Kx @ Kx
+    T = np.eye(4)
+    T[:3, :3] = R
+    T[:3, 3] = [0.004, -0.002, 0.003]
+    return {"depth": np.ascontiguousarray(depth, np.float32), "T21": np.ascontiguousarray(T, np.float32)}
+
+
+def refpin_gpu_config(c):
+    """or_config of the refpin_gpu case: float TSDF storage (the reference's)"""
+    oc = O.OrConfig()
+    oc.width, oc.height = int(c["width"]), int(c["height"])
+    oc.fx, oc.fy, oc.cx, oc.cy = float(c["fx"]), float(c["fy"]), float(c["cx"]), float(c["cy"])
+    oc.levels = 3
+    for k in range(3):
+        oc.dim[k] = int(c["dim"])
+        oc.origin[k] = float(c["origin"][k])
+        oc.icp_iters[k] = (10, 5, 4)[k]
+    oc.voxel_size, oc.mu, oc.max_w = float(c["voxel_size"]), float(c["mu"]), float(c["max_w"])
+    oc.th_icp, oc.cos_normal, oc.tsdf_store, oc.reduce_mode, oc.depth_scale = 0.01, -3.0, 0, 1, 0.001
+    return oc
+
+
 if __name__ == "__main__":
     refpin()
     refpin_cuda()
+    refpin_gpu()
     seq_small()
     print("fixtures written to", OUT)

@@ -160,3 +160,145 @@ def test_live_reference_device_math(built):
             assert r1 == lib.or_prim_bilinear3(xf, yf, w, h, _p(mp), norm, _p(o2))
             if r1:
                 assert np.array_equal(_bits(o1), _bits(o2))
+
+
+# ---- the reference's renderer and integrator, run as host code ----------------
+GOLD_GPU = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refpin_gpu.npz")
+
+
+def _gpu_case_config(g):
+    sys_path_golden = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    import sys
+    if sys_path_golden not in sys.path:
+        sys.path.insert(0, sys_path_golden)
+    import gen_golden
+    return gen_golden.refpin_gpu_config(dict(width=int(g["cfg_w"]), height=int(g["cfg_h"]), fx=float(g["cfg_f"]),
+                                             fy=float(g["cfg_f"]), cx=int(g["cfg_w"]) / 2.0, cy=int(g["cfg_h"]) / 2.0,
+                                             dim=int(g["cfg_dim"]), origin=g["cfg_origin"],
+                                             voxel_size=float(g["cfg_vox"]), mu=float(g["cfg_mu"]),
+                                             max_w=float(g["cfg_maxw"])))
+
+
+def test_integration_and_raycast_match_the_reference_kernels_bit_for_bit(built):
+    """The oracle's TSDF / weight / colour update and its ray-cast maps equal
+    those of the reference's own g_fvsc + g_ctvc and g_rmi kernels (their
+    sources run as host code), frame by frame and level by level.  The
+    colour image has no zero texel and the depth frame a zero border, so
+    every colour sample interpolates (where one cannot, the reference blends
+    an uninitialised value and the oracle keeps the colour)."""
+    g = np.load(GOLD_GPU)
+    oc = _gpu_case_config(g)
+    vol = O.Volume(oc)
+    for k in range(2):
+        T = g["T"][k]
+        vol.integrate_color(g["depth"][k], g["rgb"][k], T, O.pose_inverse(T))
+        t, w = vol.get()
+        assert np.array_equal(w, g["weight"][k].astype(np.uint16)), k
+        assert np.array_equal(_bits(t), _bits(g["tsdf"][k])), k
+        assert np.array_equal(vol.get_color().reshape(-1), g["colour"][k]), k
+    T = g["T"][2]
+    cam = O.camera_center(T)
+    for l in range(3):
+        d, v, n, img = vol.raycast(l, T, O.pose_inverse(T), cam, np.array([0, 0, -1], np.float32))
+        assert (d > 0).sum() > 20
+        assert np.array_equal(_bits(d.reshape(-1)), _bits(g["depth%d" % l])), l
+        assert np.array_equal(_bits(v.reshape(-1)), _bits(g["vertex%d" % l])), l
+        assert np.array_equal(_bits(n.reshape(-1)), _bits(g["normal%d" % l])), l
+        assert np.array_equal(img.reshape(-1), g["img%d" % l]), l
+
+
+def test_live_reference_kernels(built):
+    """where the reference tree is mounted: a 160x120 sequence into a 96^3 cube,
+    the oracle against the reference's renderer and integrator run live"""
+    libs = O.load_ref_pin_gpu()
+    if libs is None:
+        pytest.skip("reference tree not mounted on this host")
+    rr, ri, rt = libs
+    import vs_scanner as V
+
+    w, h, dim = 160, 120, 96
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=4, seed=5, dropout_iid=0.01)
+    depth_mm, rgb, gt, centre = V.synth_generate_rgb(sc)
+    origin, vox = V.cube_around(centre, 0.75, dim)
+    oc = _gpu_case_config(dict(cfg_w=w, cfg_h=h, cfg_f=f, cfg_dim=dim, cfg_origin=np.array(origin, np.float32),
+                               cfg_vox=vox, cfg_mu=0.03, cfg_maxw=100.0))
+    geo = np.zeros(5, np.float32)
+    O.load().or_config_geometry(ctypes.byref(oc), _p(geo))
+    K0 = np.array([oc.fx, oc.fy, oc.cx, oc.cy], np.float32)
+    dims, org, cen = np.array([dim] * 3, np.int32), np.array(list(oc.origin), np.float32), np.ascontiguousarray(geo[:3])
+    n = dim ** 3
+    t_ref, w_ref, c_ref = np.ones(n, np.float32), np.zeros(n, np.uint8), np.zeros(3 * n, np.uint8)
+    vol = O.Volume(oc)
+    for k in range(3):
+        raw = np.ascontiguousarray(O.depth_to_m(depth_mm[k]), np.float32)
+        raw[0, :] = raw[-1, :] = raw[:, 0] = raw[:, -1] = 0.0
+        img = np.ascontiguousarray(np.maximum(rgb[k], 1), np.uint8)
+        T = np.ascontiguousarray(gt[k], np.float32)
+        Ti = np.ascontiguousarray(O.pose_inverse(T))
+        vol.integrate_color(raw, img, T, Ti)
+        ri.ref_integrate_color(w, h, _p(K0), _p(dims), _p(org), _p(cen), oc.voxel_size, oc.mu, oc.max_w, _p(t_ref),
+                               _p(w_ref), _p(c_ref), _p(raw), _p(img), _p(T), _p(Ti))
+        t, wt = vol.get()
+        assert np.array_equal(wt, w_ref.astype(np.uint16)) and np.array_equal(_bits(t), _bits(t_ref)), k
+        assert np.array_equal(vol.get_color().reshape(-1), c_ref), k
+    T = np.ascontiguousarray(gt[3], np.float32)
+    Ti = np.ascontiguousarray(O.pose_inverse(T))
+    cam = np.ascontiguousarray(O.camera_center(T), np.float32)
+    light = np.array([0, 0, -1], np.float32)
+    t, wt = vol.get()
+    for l in range(3):
+        lw, lh = w >> l, h >> l
+        d, v, nn, im = (np.zeros(lw * lh, np.float32), np.zeros(3 * lw * lh, np.float32),
+                        np.zeros(3 * lw * lh, np.float32), np.zeros(lw * lh, np.uint8))
+        rr.ref_render_icp(w, h, _p(K0), l, _p(dims), _p(org), _p(cen), oc.voxel_size, oc.mu, oc.max_w,
+                          _p(np.ascontiguousarray(t)), _p(wt.astype(np.uint8)), _p(T), _p(Ti), _p(cam), _p(light),
+                          _p(d), _p(v), _p(nn), _p(im))
+        od, ov, on, oi = vol.raycast(l, T, Ti, cam, light)
+        assert (d > 0).sum() > 300 >> (2 * l)
+        for a, b in ((od, d), (ov, v), (on, nn)):
+            assert np.array_equal(_bits(a.reshape(-1)), _bits(b)), l
+        assert np.array_equal(oi.reshape(-1), im), l
+        if l == 0:
+            # the per-pixel ICP term of the next frame against these maps
+            icp = _icp_case(np.ascontiguousarray(O.depth_to_m(depth_mm[3]), np.float32))
+            ATA, ATb, ok = np.zeros((w * h, 36), np.float32), np.zeros((w * h, 6), np.float32), np.zeros(w * h, np.uint8)
+            rt.ref_icp_terms(w, h, _p(K0), _p(icp["depth"]), _p(d), _p(v), _p(nn), _p(icp["T21"]), 0.01, _p(ATA),
+                             _p(ATb), _p(ok))
+            assert ok.sum() > 1000
+            _check_icp_terms(w, h, K0, icp["depth"], v, nn, icp["T21"], ATA, ATb, ok)
+
+
+def _icp_case(depth):
+    import sys
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import gen_golden
+    return gen_golden.icp_case(depth)
+
+
+def _check_icp_terms(w, h, K, depth, vtx, nrm, T21, ATA, ATb, ok):
+    """the oracle's per-pixel A, b give the reference's ATA = A A^T and
+    ATb = A b (each product rounded once, in float32) and the same pixels"""
+    lib = O.load()
+    A, b = np.zeros(6, np.float32), np.zeros(1, np.float32)
+    args = [_p(np.ascontiguousarray(a, np.float32)) for a in (K, depth, vtx, nrm, T21)]
+    for y in range(h):
+        for x in range(w):
+            i = y * w + x
+            r = lib.or_prim_icp_term(x, y, w, h, *args[:4], args[4], 0.01, _p(A), _p(b))
+            assert r == ok[i], (x, y)
+            if r:
+                assert np.array_equal(_bits(np.outer(A, A).astype(np.float32).reshape(-1)), _bits(ATA[i])), (x, y)
+                assert np.array_equal(_bits((A * b[0]).astype(np.float32)), _bits(ATb[i])), (x, y)
+
+
+def test_icp_terms_match_the_reference_kernel_bit_for_bit(built):
+    """the per-pixel term of the reference's d_cssfp (z_yooji_cuda_pose_tracker.cu:279-395)
+    against level-1 model maps the reference rendered"""
+    g = np.load(GOLD_GPU)
+    w, h = int(g["cfg_w"]) >> 1, int(g["cfg_h"]) >> 1
+    assert g["icp_ok"].sum() > 20
+    _check_icp_terms(w, h, g["icp_K"], g["icp_depth"], g["vertex1"], g["normal1"], g["icp_T21"], g["icp_ATA"],
+                     g["icp_ATb"], g["icp_ok"])
