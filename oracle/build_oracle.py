@@ -6,9 +6,9 @@
 * oracle/_ref/libref_pin_cuda.so -- the reference's own _yooji_cuda_math.h
   (per-pixel / per-voxel helpers) compiled as host C++ with the stand-ins of
   oracle/ref_shim/, likewise only where the tree is present.
-* oracle/_ref/libref_pin_render.so, libref_pin_integ.so -- the reference's own
-  renderer and integrator sources run as host code (see build_ref_pin_gpu),
-  likewise only where the tree is present.
+* oracle/_ref/libref_pin_{render,integ,track,imgproc}.so -- the reference's own
+  renderer, integrator, tracker and bilateral-filter sources run as host code
+  (see build_ref_pin_gpu), likewise only where the tree is present.
 
 No -march flags: the same source must build on x86-64 and aarch64.
 -ffp-contract=off keeps GCC from fusing multiply-adds (the CUDA side builds
@@ -75,12 +75,13 @@ REF_STAC = os.path.dirname(REF_UTIL)
 _LAUNCH = r"(\w+)\s*<<<([^<>]*)>>>\s*\("
 _GPU_SOURCES = {"math": "Util/z_yooji_cuda_math.cu", "renderer": "Engine/GPU/z_yooji_cuda_tsdf_renderer.cu",
                 "integrator": "Engine/GPU/z_yooji_cuda_volume_integrator.cu",
-                "tracker": "Engine/GPU/z_yooji_cuda_pose_tracker.cu"}
+                "tracker": "Engine/GPU/z_yooji_cuda_pose_tracker.cu", "imgproc": "Engine/GPU/z_yooji_cuda_img_proc.cu"}
 
 
 def build_ref_pin_gpu(force=False):
-    """The reference's renderer and integrator run as host code.  Returns
-    {"render": path, "integ": path, "track": path}, or None when the reference tree is absent.
+    """The reference's renderer, integrator, tracker and bilateral filter run
+    as host code.  Returns {"render", "integ", "track", "imgproc": path}, or
+    None when the reference tree is absent.
 
     The launch syntax is the only text changed: each source is read from the
     reference tree, its `<<<...>>>` launches are turned into calls of the host
@@ -93,7 +94,8 @@ def build_ref_pin_gpu(force=False):
     shim = os.path.join(HERE, "ref_shim", "gpu")
     outs = {"render": os.path.join(HERE, "_ref", "libref_pin_render.so"),
             "integ": os.path.join(HERE, "_ref", "libref_pin_integ.so"),
-            "track": os.path.join(HERE, "_ref", "libref_pin_track.so")}
+            "track": os.path.join(HERE, "_ref", "libref_pin_track.so"),
+            "imgproc": os.path.join(HERE, "_ref", "libref_pin_imgproc.so")}
     srcs = [os.path.join(REF_STAC, v) for v in _GPU_SOURCES.values()]
     deps = srcs + [os.path.join(HERE, f) for f in ("ref_pin_gpu.cpp", "ref_gpu_runtime.cpp")] + \
         [os.path.join(shim, f) for f in os.listdir(shim)]
@@ -119,7 +121,8 @@ def build_ref_pin_gpu(force=False):
                                "-o", objs[name]])
     objs["rt"] = os.path.join(gen, "rt.o")
     subprocess.check_call([CXX] + cflags + ["-I", shim, "-c", os.path.join(HERE, "ref_gpu_runtime.cpp"), "-o", objs["rt"]])
-    for key, macro in (("render", "REF_PIN_RENDER"), ("integ", "REF_PIN_INTEG"), ("track", "REF_PIN_TRACK")):
+    for key, macro in (("render", "REF_PIN_RENDER"), ("integ", "REF_PIN_INTEG"), ("track", "REF_PIN_TRACK"),
+                       ("imgproc", "REF_PIN_IMGPROC")):
         o = os.path.join(gen, key + ".o")
         subprocess.check_call([CXX] + cflags + inc + ["-D" + macro, "-c", "-x", "c++",
                                os.path.join(HERE, "ref_pin_gpu.cpp"), "-o", o])

@@ -160,15 +160,16 @@ _ref_gpu = None
 
 
 def load_ref_pin_gpu():
-    """The reference's renderer, integrator and tracker run as host code:
-    (render, integ, track) libraries, or None when the reference tree is absent."""
+    """The reference's renderer, integrator, tracker and bilateral filter run as
+    host code: (render, integ, track, imgproc) libraries, or None when the
+    reference tree is absent."""
     global _ref_gpu
     if _ref_gpu is None:
         import build_oracle as _b
         paths = _b.build_ref_pin_gpu()
         if paths is None:
             return None
-        r, i, t = (ctypes.CDLL(paths[k]) for k in ("render", "integ", "track"))
+        r, i, t, b = (ctypes.CDLL(paths[k]) for k in ("render", "integ", "track", "imgproc"))
         P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
         r.ref_render_icp.restype = I
         r.ref_render_icp.argtypes = [I, I, P, I, P, P, P, F, F, F, P, P, P, P, P, P, P, P, P, P]
@@ -176,7 +177,9 @@ def load_ref_pin_gpu():
         i.ref_integrate_color.argtypes = [I, I, P, P, P, P, F, F, F, P, P, P, P, P, P, P]
         t.ref_icp_terms.restype = None
         t.ref_icp_terms.argtypes = [I, I, P, P, P, P, P, P, F, P, P, P]
-        _ref_gpu = (r, i, t)
+        b.ref_bilateral.restype = None
+        b.ref_bilateral.argtypes = [I, I, P, P]
+        _ref_gpu = (r, i, t, b)
     return _ref_gpu
 
 

@@ -26,6 +26,16 @@ cudaError_t cudaMemcpy(void* d, const void* s, size_t n, cudaMemcpyKind) {
   if (n) std::memmove(d, s, n);
   return 0;
 }
+cudaError_t cudaMallocPitch(void** p, size_t* pitch, size_t wbytes, size_t h) {
+  *pitch = wbytes;
+  return cudaMalloc(p, wbytes * h);
+}
+cudaError_t cudaMemcpy2D(void* d, size_t dpitch, const void* s, size_t spitch, size_t wbytes, size_t h,
+                         cudaMemcpyKind) {
+  for (size_t r = 0; r < h; r++)
+    std::memmove(static_cast<char*>(d) + r * dpitch, static_cast<const char*>(s) + r * spitch, wbytes);
+  return 0;
+}
 cudaError_t cudaMemset(void* d, int v, size_t n) {
   std::memset(d, v, n);
   return 0;

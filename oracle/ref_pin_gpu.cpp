@@ -14,6 +14,9 @@
 //     d_cssfp_Compute_Single_Summand_with_Forward_Params of
 //     z_yooji_cuda_pose_tracker.cu; its block reductions use shared memory
 //     and barriers, which a one-thread-at-a-time host loop cannot run)
+//   oracle/_ref/libref_pin_imgproc.so (REF_PIN_IMGPROC: the bilateral filter
+//     of z_yooji_cuda_img_proc.cu through LGKvImageProcessor, its texture
+//     reference given by the texture stand-in of ref_gpu_shim.h)
 // The reference's own host code then runs unchanged on host memory: the cube
 // class, ip_Initialize_Parameters, rmi_Render_Maps_for_ICP and
 // cdtocc_Convert_Depth_to_TSDF_on_Cube_with_Color with their kernels
@@ -92,5 +95,16 @@ extern "C" void ref_icp_terms(int W, int H, const float* K, const float* depth_t
                   ? 1
                   : 0;
     }
+}
+#endif
+
+#if defined(REF_PIN_IMGPROC)
+#include "imgproc.cu.cpp"
+
+// the reference's bilateral filter of one depth frame (metres in, metres out)
+extern "C" void ref_bilateral(int W, int H, const float* depth, float* out) {
+  LGKvImageProcessor ip;
+  ip.bfd_Bilateral_Filter_Depth_Host(out, depth, W, H);
+  ip.r_Release();
 }
 #endif

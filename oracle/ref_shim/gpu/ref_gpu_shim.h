@@ -63,6 +63,9 @@ inline float __fadd_rn(float a, float b) { return a + b; }
 inline float __fmul_rn(float a, float b) { return a * b; }
 inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
 inline float __int2float_rn(int x) { return (float)x; }
+// the fast exponential's error bound is the GPU's own; on the host it is the
+// correctly rounded expf of the C library (the oracle's choice as well)
+inline float __expf(float x) { return std::exp(x); }
 
 // _yooji_cuda_math.hpp:98 (GKvMatrix<T>::to_host) names an undeclared
 // `out_vol`; MSVC never checks the uninstantiated template, GCC needs the name
@@ -97,6 +100,63 @@ cudaError_t cudaMemcpyFromSymbol(void* dst, const T& sym, size_t n, size_t off =
   return 0;
 }
 #define checkCudaErrors(x) (x)
+// pitched buffers: the pitch is the row's own size (no alignment padding), so
+// a texture bound with pitch 4 W (z_yooji_cuda_img_proc.cu:305) reads the rows
+// the pitched copy wrote, the dense layout the filter means to use
+cudaError_t cudaMallocPitch(void** p, size_t* pitch, size_t wbytes, size_t h);
+cudaError_t cudaMemcpy2D(void* d, size_t dpitch, const void* s, size_t spitch, size_t wbytes, size_t h,
+                         cudaMemcpyKind);
+
+// CUDA 8 texture references, as far as the bilateral filter uses them.
+// tex2D follows the texture-fetching rules of the CUDA C programming guide
+// for unnormalised coordinates: point sampling reads texel (floor x, floor y);
+// linear filtering reads the 2x2 texels around (x - 0.5, y - 0.5) with
+// weights a, b of 8 fractional bits as (1-b)((1-a) T00 + a T10) +
+// b((1-a) T01 + a T11); addresses clamp to the edge (wrap and mirror apply to
+// normalised coordinates only).  At the integer coordinates the filter uses,
+// a = b = 1/2 and every product is exact, so the tap is the mean of 2x2
+// texels whatever precision the texture unit blends in.
+enum cudaTextureReadMode { cudaReadModeElementType, cudaReadModeNormalizedFloat };
+enum cudaTextureAddressMode { cudaAddressModeWrap, cudaAddressModeClamp, cudaAddressModeMirror, cudaAddressModeBorder };
+enum cudaTextureFilterMode { cudaFilterModePoint, cudaFilterModeLinear };
+template <class T, int D = 1, cudaTextureReadMode M = cudaReadModeElementType>
+struct texture {
+  int normalized = 0;
+  cudaTextureFilterMode filterMode = cudaFilterModePoint;
+  cudaTextureAddressMode addressMode[3] = {cudaAddressModeClamp, cudaAddressModeClamp, cudaAddressModeClamp};
+  const char* base = nullptr;
+  long w = 0, h = 0;
+  size_t pitch = 0;
+};
+template <class T>
+cudaChannelFormatDesc cudaCreateChannelDesc() {
+  return cudaChannelFormatDesc{int(8 * sizeof(T)), 0, 0, 0, 2};
+}
+template <class T, int D, cudaTextureReadMode M>
+cudaError_t cudaBindTexture2D(size_t* off, texture<T, D, M>& t, const void* p, const cudaChannelFormatDesc&, size_t w,
+                              size_t h, size_t pitch) {
+  if (off) *off = 0;
+  t.base = static_cast<const char*>(p), t.w = (long)w, t.h = (long)h, t.pitch = pitch;
+  return 0;
+}
+template <class T, int D, cudaTextureReadMode M>
+cudaError_t cudaUnbindTexture(texture<T, D, M>& t) {
+  t.base = nullptr;
+  return 0;
+}
+template <class T, int D, cudaTextureReadMode M>
+T tex2D(const texture<T, D, M>& t, float x, float y) {
+  auto at = [&](long i, long j) {
+    i = i < 0 ? 0 : (i >= t.w ? t.w - 1 : i);
+    j = j < 0 ? 0 : (j >= t.h ? t.h - 1 : j);
+    return *reinterpret_cast<const T*>(t.base + (size_t)j * t.pitch + (size_t)i * sizeof(T));
+  };
+  if (t.filterMode == cudaFilterModePoint) return at((long)std::floor(x), (long)std::floor(y));
+  const float xb = x - 0.5f, yb = y - 0.5f, fi = std::floor(xb), fj = std::floor(yb);
+  const float a = std::nearbyint((xb - fi) * 256.0f) / 256.0f, b = std::nearbyint((yb - fj) * 256.0f) / 256.0f;
+  const long i = (long)fi, j = (long)fj;
+  return (1.0f - b) * ((1.0f - a) * at(i, j) + a * at(i + 1, j)) + b * ((1.0f - a) * at(i, j + 1) + a * at(i + 1, j + 1));
+}
 
 // a kernel launch `k<<<grid, block>>>(args)` becomes
 // `vs_launch(grid, block, [&](auto&&... a) { k(a...); })(args)`: every thread

@@ -173,7 +173,7 @@ def refpin_gpu():
     libs = O.load_ref_pin_gpu()
     if libs is None:
         raise SystemExit("the reference tree is not mounted; refpin_gpu.npz cannot be regenerated")
-    rr, ri, rt = libs
+    rr, ri, rt, rb = libs
     import vs_scanner as V
     p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
     w, h, dim, size = 80, 60, 48, 0.75
@@ -230,10 +230,32 @@ def refpin_gpu():
                      p(icp["T21"]), 0.01, p(ATA), p(ATb), p(ok))
     maps.update({"icp_depth": icp["depth"], "icp_T21": icp["T21"], "icp_K": K1, "icp_ATA": ATA, "icp_ATb": ATb,
                  "icp_ok": ok})
+    # the bilateral filter of the raw frame with holes of each kind
+    bil = bilateral_input(O.depth_to_m(depth_mm[0]))
+    out = np.zeros_like(bil)
+    rb.ref_bilateral(w, h, p(bil), p(out))
+    maps.update({"bil_in": bil, "bil_out": out})
     np.savez_compressed(os.path.join(OUT, "refpin_gpu.npz"), cfg_w=w, cfg_h=h, cfg_f=f, cfg_dim=dim,
                         cfg_origin=cfg["origin"], cfg_vox=vox, cfg_mu=0.03, cfg_maxw=100.0, depth=np.stack(depths),
                         rgb=np.stack(imgs), T=np.ascontiguousarray(gt[:3], np.float32), tsdf=np.stack(tsdf),
                         weight=np.stack(weight), colour=np.stack(colour), **maps)
+
+
+def bilateral_input(depth):
+    """a depth frame (metres) with a 30 cm step, single zero texels and zero
+    lines one texel wide (averaged into the taps), and 2x2 zero blocks and
+    zero lines two texels wide (each makes a hole), one in a corner"""
+    d = np.array(depth, np.float32)
+    h, w = d.shape
+    d[:, (2 * w) // 3:] += 0.3
+    d[7, 9] = d[30, 41] = 0.0
+    d[h // 3, :] = 0.0
+    d[:, w // 4] = 0.0
+    d[20:22, 20:22] = 0.0
+    d[h - 2:h, w - 2:w] = 0.0
+    d[h // 2:h // 2 + 2, :] = 0.0
+    d[:, w // 2:w // 2 + 2] = 0.0
+    return np.ascontiguousarray(d)
 
 
 def icp_case(depth):

@@ -213,7 +213,7 @@ def test_live_reference_kernels(built):
     libs = O.load_ref_pin_gpu()
     if libs is None:
         pytest.skip("reference tree not mounted on this host")
-    rr, ri, rt = libs
+    rr, ri, rt, rb = libs
     import vs_scanner as V
 
     w, h, dim = 160, 120, 96
@@ -302,3 +302,45 @@ def test_icp_terms_match_the_reference_kernel_bit_for_bit(built):
     assert g["icp_ok"].sum() > 20
     _check_icp_terms(w, h, g["icp_K"], g["icp_depth"], g["vertex1"], g["normal1"], g["icp_T21"], g["icp_ATA"],
                      g["icp_ATb"], g["icp_ok"])
+
+
+def test_bilateral_matches_the_reference_kernel_bit_for_bit(built):
+    """the oracle's bilateral filter against the reference's d_bilateral_filter
+    (z_yooji_cuda_img_proc.cu:103-141, run as host code with the documented
+    texture-fetch rules for its linear-filtered texture) on a frame with
+    single zero texels, 2x2 holes, zero lines and a depth step"""
+    g = np.load(GOLD_GPU)
+    w, h = int(g["cfg_w"]), int(g["cfg_h"])
+    x = np.ascontiguousarray(g["bil_in"], np.float32)
+    out = np.zeros_like(x)
+    O.load().or_bilateral(_p(x), w, h, _p(out))
+    assert (g["bil_out"] == 0).sum() > 100 and (g["bil_out"] > 0).sum() > 2000
+    assert np.array_equal(_bits(out), _bits(g["bil_out"]))
+
+
+def test_live_reference_bilateral(built):
+    """where the reference tree is mounted: ragged and VGA frames"""
+    libs = O.load_ref_pin_gpu()
+    if libs is None:
+        pytest.skip("reference tree not mounted on this host")
+    rb = libs[3]
+    import vs_scanner as V
+
+    for (w, h, seed) in ((97, 75, 3), (170, 130, 4), (640, 480, 5)):
+        f = 285.0 * w / 320.0
+        sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=1, seed=seed, dropout_iid=0.02)
+        d = V.synth_generate(sc)[0]
+        x = _bilateral_input(O.depth_to_m(d[0]))
+        a, b = np.zeros_like(x), np.zeros_like(x)
+        rb.ref_bilateral(w, h, _p(x), _p(a))
+        O.load().or_bilateral(_p(x), w, h, _p(b))
+        assert np.array_equal(_bits(a), _bits(b)), (w, h)
+
+
+def _bilateral_input(depth):
+    import sys
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import gen_golden
+    return gen_golden.bilateral_input(depth)
