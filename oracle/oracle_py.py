@@ -177,6 +177,8 @@ def load_ref_pin_gpu():
         i.ref_integrate_color.argtypes = [I, I, P, P, P, P, F, F, F, P, P, P, P, P, P, P]
         t.ref_icp_terms.restype = None
         t.ref_icp_terms.argtypes = [I, I, P, P, P, P, P, P, F, P, P, P]
+        t.ref_track_pose.restype = I
+        t.ref_track_pose.argtypes = [I, I, P, F, P, P, P, P, P, P, P]
         b.ref_bilateral.restype = None
         b.ref_bilateral.argtypes = [I, I, P, P]
         _ref_gpu = (r, i, t, b)

@@ -1,6 +1,9 @@
 // Host definitions behind ref_shim/gpu/ref_gpu_shim.h: the launch variables
 // and the runtime calls on host memory (TEST INFRASTRUCTURE ONLY).
+#include <ucontext.h>
+
 #include <set>
+#include <vector>
 
 #include "ref_gpu_shim.h"
 
@@ -43,3 +46,57 @@ cudaError_t cudaMemset(void* d, int v, size_t n) {
 cudaError_t cudaDeviceSynchronize() { return 0; }
 cudaError_t cudaGetLastError() { return 0; }
 const char* cudaGetErrorString(cudaError_t) { return "no error"; }
+
+// ---- cooperative threads of one block (kernels with barriers) --------------
+bool vs_block_threads = false;
+namespace {
+struct BlockThread {
+  ucontext_t ctx;
+  uint3_ tid;
+  bool done;
+};
+constexpr size_t kStack = 256 * 1024;
+ucontext_t g_sched;
+std::vector<BlockThread> g_thr;
+std::vector<std::vector<char>> g_stacks;
+int g_cur = -1;
+void (*g_body)(void*);
+void* g_arg;
+void thread_entry() {
+  g_body(g_arg);
+  g_thr[g_cur].done = true;  // returning resumes g_sched through uc_link
+}
+}  // namespace
+
+void __syncthreads() {
+  if (g_cur >= 0) swapcontext(&g_thr[g_cur].ctx, &g_sched);
+}
+
+void vs_run_block_threads(const dim3& b, void (*body)(void*), void* arg) {
+  const int n = (int)(b.x * b.y * b.z);
+  g_thr.resize(n);
+  if ((int)g_stacks.size() < n) g_stacks.resize(n);
+  g_body = body, g_arg = arg;
+  for (int i = 0; i < n; i++) {
+    BlockThread& t = g_thr[i];
+    t.tid.x = i % b.x, t.tid.y = (i / b.x) % b.y, t.tid.z = i / (b.x * b.y);
+    t.done = false;
+    g_stacks[i].resize(kStack);
+    getcontext(&t.ctx);
+    t.ctx.uc_stack.ss_sp = g_stacks[i].data();
+    t.ctx.uc_stack.ss_size = kStack;
+    t.ctx.uc_link = &g_sched;
+    makecontext(&t.ctx, thread_entry, 0);
+  }
+  for (bool running = true; running;) {
+    running = false;
+    for (int i = n - 1; i >= 0; i--) {
+      if (g_thr[i].done) continue;
+      threadIdx = g_thr[i].tid;
+      g_cur = i;
+      swapcontext(&g_sched, &g_thr[i].ctx);
+      running |= !g_thr[i].done;
+    }
+  }
+  g_cur = -1;
+}

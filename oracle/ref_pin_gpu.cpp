@@ -12,8 +12,9 @@
 //   oracle/_ref/libref_pin_integ.so   (REF_PIN_INTEG)
 //   oracle/_ref/libref_pin_track.so   (REF_PIN_TRACK: the per-pixel ICP term
 //     d_cssfp_Compute_Single_Summand_with_Forward_Params of
-//     z_yooji_cuda_pose_tracker.cu; its block reductions use shared memory
-//     and barriers, which a one-thread-at-a-time host loop cannot run)
+//     z_yooji_cuda_pose_tracker.cu, and the whole of tp_Track_Pose, whose
+//     block reductions use shared memory and barriers and so run as
+//     cooperative block threads, vs_block_threads of the shim)
 //   oracle/_ref/libref_pin_imgproc.so (REF_PIN_IMGPROC: the bilateral filter
 //     of z_yooji_cuda_img_proc.cu through LGKvImageProcessor, its texture
 //     reference given by the texture stand-in of ref_gpu_shim.h)
@@ -95,6 +96,42 @@ extern "C" void ref_icp_terms(int W, int H, const float* K, const float* depth_t
                   ? 1
                   : 0;
     }
+}
+
+// the reference's tp_Track_Pose: t0 maps (model depth / vertex / normal of
+// each level, the reference's float3 layout), t1 depth levels, the previous
+// pose T_gc (row-major 4x4) and an optional initial increment T_12; writes
+// the tracked T_gc and returns 1, or returns 0 where the solve failed
+extern "C" int ref_track_pose(int W, int H, const float* K0, float th_icp, const float* const* depth_t1,
+                              const float* const* depth_t0, const float* const* vtx3_t0,
+                              const float* const* nrm3_t0, const float* T_gc_prev, const float* init_T12,
+                              float* T_gc_out) {
+  GKvTrackingState ts;
+  GKvRgbdFrame fr;
+  if (!ts.create(Vector2i(W, H)) || !fr.create(Vector2i(W, H))) return -1;
+  for (int l = 0; l < GK_LEVEL_OF_IMAGE_PYRAMID; l++) {
+    const size_t n = (size_t)(W >> l) * (H >> l);
+    std::memcpy(ts.vp_map_depth(l), depth_t0[l], n * sizeof(float));
+    std::memcpy(ts.vp_map_vertex(l), vtx3_t0[l], 3 * n * sizeof(float));
+    std::memcpy(ts.vp_map_normal(l), nrm3_t0[l], 3 * n * sizeof(float));
+    std::memcpy(fr.vp_map_depth(l), depth_t1[l], n * sizeof(float));
+  }
+  GKvMatrixFloat prev, init;
+  prev.create(4, 4, 1);
+  std::memcpy(prev.vp(), T_gc_prev, 16 * sizeof(float));
+  ts.set_transform(&prev, false);
+  if (init_T12) {
+    init.create(4, 4, 1);
+    std::memcpy(init.vp(), init_T12, 16 * sizeof(float));
+  }
+  LGKvPoseTracker tr;
+  tr.ip_Initialize_Parameters(W, H, K0[0], K0[1], K0[2], K0[3], th_icp);
+  vs_block_threads = true;
+  const bool ok = tr.tp_Track_Pose(&ts, &fr, init_T12 ? &init : nullptr);
+  vs_block_threads = false;
+  std::fflush(stdout);  // the tracker prints ATA every iteration
+  std::memcpy(T_gc_out, ts.vp_T_gc(), 16 * sizeof(float));
+  return ok ? 1 : 0;
 }
 #endif
 

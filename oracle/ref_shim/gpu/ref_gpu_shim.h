@@ -56,7 +56,9 @@ struct float3 {
 struct float4 {
   float x, y, z, w;
 };
-inline void __syncthreads() {}
+// a barrier: a no-op for the one-thread-at-a-time loop, a switch back to the
+// block's scheduler when the block runs as cooperative threads (below)
+void __syncthreads();
 inline int __float2int_rn(float x) { return (int)std::nearbyint(x); }  // default rounding mode: half to even
 // IEEE round-to-nearest operations by their definition
 inline float __fadd_rn(float a, float b) { return a + b; }
@@ -158,10 +160,22 @@ T tex2D(const texture<T, D, M>& t, float x, float y) {
   return (1.0f - b) * ((1.0f - a) * at(i, j) + a * at(i + 1, j)) + b * ((1.0f - a) * at(i, j + 1) + a * at(i + 1, j + 1));
 }
 
+// Kernels with barriers (vs_block_threads set by the harness around their
+// launches) run each block as cooperative threads on their own stacks: every
+// thread runs up to its next __syncthreads, then the next thread, round after
+// round, so all threads of the block pass each barrier together.  Between two
+// barriers the threads run in descending order of their linear index
+// (x + y X + z X Y).  A tree step `if (c < i) s[c] += s[c + i]` then reads each
+// s[c + i] after its own thread has finished every earlier step and before any
+// later one, which is the lock-step result that a warp-synchronous tail with
+// no barrier means to compute.
+extern bool vs_block_threads;
+void vs_run_block_threads(const dim3& b, void (*body)(void*), void* arg);
+
 // a kernel launch `k<<<grid, block>>>(args)` becomes
 // `vs_launch(grid, block, [&](auto&&... a) { k(a...); })(args)`: every thread
-// of the grid runs the kernel body in turn (the kernels pinned here have no
-// shared memory and no barriers, so the order is immaterial)
+// of the grid runs the kernel body in turn (kernels without shared memory or
+// barriers), or each block runs as cooperative threads (vs_block_threads)
 template <class F>
 struct VsLaunch {
   dim3 g, b;
@@ -170,9 +184,15 @@ struct VsLaunch {
   void operator()(A&&... a) {
     gridDim = g;
     blockDim = b;
+    auto body = [&]() { f(a...); };
+    using B = decltype(body);
     for (unsigned bz = 0; bz < g.z; bz++)
       for (unsigned by = 0; by < g.y; by++)
         for (unsigned bx = 0; bx < g.x; bx++)
+          if (vs_block_threads) {
+            blockIdx.x = bx, blockIdx.y = by, blockIdx.z = bz;
+            vs_run_block_threads(b, [](void* p) { (*static_cast<B*>(p))(); }, &body);
+          } else
           for (unsigned tz = 0; tz < b.z; tz++)
             for (unsigned ty = 0; ty < b.y; ty++)
               for (unsigned tx = 0; tx < b.x; tx++) {

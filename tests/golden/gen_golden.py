@@ -271,6 +271,70 @@ def icp_case(depth):
     return {"depth": np.ascontiguousarray(depth, np.float32), "T21": np.ascontiguousarray(T, np.float32)}
 
 
+def track_case(w, h, dim=128, size=0.75, seed=7):
+    """the tracking case of refpin_track: frames 0 and 1 integrated at their
+    true poses into a float cube, model maps ray-cast at pose 1, frame 2
+    filtered into the input pyramid (all by the oracle, whose integration,
+    ray-cast and bilateral filter equal the reference's bit for bit).
+    Returns (or_config with the reference's tracker settings, raw frames in
+    mm, true poses, input depth levels, model depth / vertex / normal levels)."""
+    import vs_scanner as V
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=3, seed=seed, dropout_iid=0.01)
+    dmm, gt, centre = V.synth_generate(sc)
+    origin, vox = V.cube_around(centre, size, dim)
+    oc = refpin_gpu_config(dict(width=w, height=h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, dim=dim,
+                                origin=np.array(origin, np.float32), voxel_size=vox, mu=0.03, max_w=100.0))
+    # the reference's tracker: block-tree reduction, iterations {10, 7, 7},
+    # distance threshold (0.055 size)^2
+    oc.reduce_mode = 0
+    oc.th_icp = float(np.float32((0.055 * size) ** 2))
+    for k, n in enumerate((10, 7, 7)):
+        oc.icp_iters[k] = n
+    vol = O.Volume(oc)
+    for k in range(2):
+        T = np.ascontiguousarray(gt[k], np.float32)
+        vol.integrate(O.depth_to_m(dmm[k]), T, O.pose_inverse(T))
+    T1 = np.ascontiguousarray(gt[1], np.float32)
+    md, mv, mn = [], [], []
+    for l in range(3):
+        d, v, n, _ = vol.raycast(l, T1, O.pose_inverse(T1), O.camera_center(T1))
+        md.append(np.ascontiguousarray(d))
+        mv.append(np.ascontiguousarray(v))
+        mn.append(np.ascontiguousarray(n))
+    ind = [np.ascontiguousarray(O.bilateral(O.depth_to_m(dmm[2])), np.float32)]
+    for l in range(2):
+        ind.append(np.ascontiguousarray(O.pyramid_down(ind[-1]), np.float32))
+    return oc, dmm, np.ascontiguousarray(gt, np.float32), ind, md, mv, mn
+
+
+def ref_track(rt, oc, ind, md, mv, mn, T_prev, init):
+    """the reference's tp_Track_Pose on these inputs: (ok, T_gc out)"""
+    pa = lambda arrs: (ctypes.c_void_p * len(arrs))(*[a.ctypes.data for a in arrs])
+    K0 = np.array([oc.fx, oc.fy, oc.cx, oc.cy], np.float32)
+    out = np.zeros(16, np.float32)
+    init_p = None if init is None else np.ascontiguousarray(init, np.float32).ctypes.data_as(ctypes.c_void_p)
+    ok = rt.ref_track_pose(oc.width, oc.height, K0.ctypes.data_as(ctypes.c_void_p), oc.th_icp, pa(ind), pa(md),
+                           pa(mv), pa(mn), np.ascontiguousarray(T_prev, np.float32).ctypes.data_as(ctypes.c_void_p),
+                           init_p, out.ctypes.data_as(ctypes.c_void_p))
+    return ok, out.reshape(4, 4)
+
+
+def refpin_track():
+    """the reference's whole tp_Track_Pose (160x120, three levels; and level 0
+    only from an identity initial increment), its block trees run as
+    cooperative threads; about a minute"""
+    libs = O.load_ref_pin_gpu()
+    if libs is None:
+        raise SystemExit("the reference tree is not mounted; refpin_track.npz cannot be regenerated")
+    w, h = 160, 120
+    oc, dmm, gt, ind, md, mv, mn = track_case(w, h)
+    ok0, T0 = ref_track(libs[2], oc, ind, md, mv, mn, gt[1], None)
+    ok1, T1 = ref_track(libs[2], oc, ind, md, mv, mn, gt[1], np.eye(4, dtype=np.float32))
+    np.savez_compressed(os.path.join(OUT, "refpin_track.npz"), w=w, h=h, depth_mm=dmm, gt=gt, ok_levels=ok0,
+                        T_levels=T0, ok_init=ok1, T_init=T1)
+
+
 def refpin_gpu_config(c):
     """or_config of the refpin_gpu case: float TSDF storage (the reference's)"""
     oc = O.OrConfig()
@@ -290,5 +354,6 @@ if __name__ == "__main__":
     refpin()
     refpin_cuda()
     refpin_gpu()
+    refpin_track()
     seq_small()
     print("fixtures written to", OUT)

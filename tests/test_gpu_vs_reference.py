@@ -7,7 +7,9 @@ Here the sm_103a kernels take the same inputs through the C ABI and must give
 the same numbers: TSDF, weights, colour and the ray-cast maps bit for bit
 (FP32 TSDF storage, the reference's), the bilateral filter within 1e-5 m (the
 kernel uses the GPU's fast exponential where the host used expf) with the
-same holes."""
+same holes.  tests/golden/refpin_track.npz holds the pose the reference's
+tp_Track_Pose tracked; the CUDA tracker (its own reduction order, FP64 pose
+algebra) lands within 1e-4 of it from the same frames."""
 import os
 
 import numpy as np
@@ -81,3 +83,40 @@ def test_integration_and_raycast_against_the_reference_kernels(gpu):
             assert np.array_equal(_bits(gv.cpu().numpy()), _bits(g["vertex%d" % l])), l
             assert np.array_equal(_bits(gn.cpu().numpy()), _bits(g["normal%d" % l])), l
             assert np.array_equal(gi.cpu().numpy(), g["img%d" % l]), l
+
+
+def test_tracking_against_the_reference_tracker(gpu):
+    """frames 0 and 1 integrated on the GPU at their true poses, the model
+    ray-cast at pose 1, frame 2 filtered and tracked with the reference's
+    tracker settings (iterations {10, 7, 7}, distance (0.055 size)^2, no
+    normal test): the pose is the reference's within 1e-4 rad / 1e-4 m"""
+    import sys
+    import helpers
+    g = np.load(os.path.join(os.path.dirname(GOLD), "refpin_track.npz"))
+    d = os.path.dirname(GOLD)
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import gen_golden
+    w, h = int(g["w"]), int(g["h"])
+    oc = gen_golden.track_case(w, h)[0]
+    cfg = V.default_config(w, h, fx=oc.fx, fy=oc.fy, cx=oc.cx, cy=oc.cy, dim=tuple(oc.dim), origin=list(oc.origin),
+                           voxel_size=oc.voxel_size, mu=oc.mu, max_w=oc.max_w, th_icp=oc.th_icp, cos_normal=-3.0,
+                           icp_iters=(10, 7, 7), tsdf_type=V.VS_TSDF_FP32, reduce_mode=V.VS_REDUCE_FP64)
+    gt = g["gt"]
+    for init, key in ((None, "T_levels"), (np.eye(4, dtype=np.float32), "T_init")):
+        with V.Session(cfg) as s:
+            for k in range(2):
+                T = np.ascontiguousarray(gt[k], np.float32)
+                d_raw, d_gc, d_cg = _dev(O.depth_to_m(g["depth_mm"][k])), _dev(T), _dev(O.pose_inverse(T))
+                s.cdtoc_convert_depth_to_tsdf(d_raw.data_ptr(), d_gc.data_ptr(), d_cg.data_ptr())
+            s.set_pose(gt[1].astype(np.float64))
+            s.stage_raycast()
+            t = _dev(g["depth_mm"][2].astype(np.uint16).view(np.int16))
+            s.stage_filter(t.data_ptr())
+            s.sync()
+            d_init = None if init is None else _dev(init)
+            ok = s.tp_track_pose(None if d_init is None else d_init.data_ptr())
+            _, T64, _ = s.pose()
+        assert ok, key
+        assert helpers.rot_err(T64, g[key]) < 1e-4, key
+        assert helpers.trans_err(T64, g[key]) < 1e-4, key

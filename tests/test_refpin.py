@@ -344,3 +344,53 @@ def _bilateral_input(depth):
         sys.path.insert(0, d)
     import gen_golden
     return gen_golden.bilateral_input(depth)
+
+
+# ---- the reference's whole tracker (tp_Track_Pose) ----------------------------
+GOLD_TRACK = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refpin_track.npz")
+
+
+def _gen_golden():
+    import sys
+    d = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import gen_golden
+    return gen_golden
+
+
+def test_tracking_matches_the_reference_tracker_bit_for_bit(built):
+    """the oracle's ICP in the reference's reduction mode (16x16 block trees of
+    all 36 + 6 sums, block partials summed serially in float) against the
+    reference's tp_Track_Pose (z_yooji_cuda_pose_tracker.cu:790-1042, with
+    g_glsbw :548-697 run as cooperative block threads): the tracked pose over
+    the three levels, and over level 0 from an identity initial increment"""
+    g = np.load(GOLD_TRACK)
+    oc, dmm, gt, ind, md, mv, mn = _gen_golden().track_case(int(g["w"]), int(g["h"]))
+    assert np.array_equal(dmm, g["depth_mm"]) and np.array_equal(gt, g["gt"])
+    for init, ok_key, T_key in ((None, "ok_levels", "T_levels"), (np.eye(4, dtype=np.float32), "ok_init", "T_init")):
+        ok, T, info = O.track(oc, ind, mv, mn, gt[1], init_T12=init)
+        assert ok and bool(g[ok_key])
+        assert np.array_equal(_bits(T), _bits(g[T_key])), T_key
+    # a converging case: closer to the true pose of frame 2 than the start
+    import helpers
+    assert helpers.camera_centre_err(g["T_levels"], gt[2]) < 0.5 * helpers.camera_centre_err(gt[1], gt[2])
+
+
+def test_live_reference_tracker(built):
+    """where the reference tree is mounted: 80x60 from an identity increment
+    (level 0, ten iterations) and over the three levels, where the 20x15 level
+    gives too few correspondences and both fail"""
+    libs = O.load_ref_pin_gpu()
+    if libs is None:
+        pytest.skip("reference tree not mounted on this host")
+    G = _gen_golden()
+    oc, dmm, gt, ind, md, mv, mn = G.track_case(80, 60, dim=64)
+    for init in (np.eye(4, dtype=np.float32), None):
+        rok, rT = G.ref_track(libs[2], oc, ind, md, mv, mn, gt[1], init)
+        ok, T, info = O.track(oc, ind, mv, mn, gt[1], init_T12=init)
+        assert bool(rok) == ok
+        if ok:
+            assert np.array_equal(_bits(T), _bits(rT))
+        else:
+            assert np.array_equal(rT, gt[1])  # the reference leaves the pose
