@@ -174,7 +174,9 @@ def load_ref_pin_gpu():
         r.ref_render_icp.restype = I
         r.ref_render_icp.argtypes = [I, I, P, I, P, P, P, F, F, F, P, P, P, P, P, P, P, P, P, P]
         i.ref_integrate_color.restype = I
-        i.ref_integrate_color.argtypes = [I, I, P, P, P, P, F, F, F, P, P, P, P, P, P, P]
+        i.ref_integrate_color.argtypes = [I, I, P, P, P, P, F, F, F, P, P, P, P, P, P, P, P]
+        r.ref_render_variant.restype = I
+        r.ref_render_variant.argtypes = [I, I, I, P, I, P, P, P, F, F, F, P, P, P, P, P, P, P, P, P, P, P, P]
         t.ref_icp_terms.restype = None
         t.ref_icp_terms.argtypes = [I, I, P, P, P, P, P, P, F, P, P, P]
         t.ref_track_pose.restype = I

@@ -48,6 +48,37 @@ extern "C" int ref_render_icp(int W, int H, const float* K0, int level, const in
                             Vector3f(light[0], light[1], light[2]), level, depth, vtx3, nrm3, img, nullptr);
   return 1;
 }
+
+// the other renders of a colour cube: variant 0 rmis_Render_Maps_for_Scene
+// with a vertex map, 1 the same without one, 2 rmi_Render_Maps_for_ICP
+// without a vertex map at the given level; rgb_img: three planes of the image
+extern "C" int ref_render_variant(int variant, int W, int H, const float* K0, int level, const int* dim,
+                                  const float* origin, const float* center, float vox, float mu, float max_w,
+                                  const float* tsdf, const uint8_t* w, const uint8_t* rgb, const float* T_gc,
+                                  const float* T_cg, const float* cam, const float* light, float* depth, float* vtx3,
+                                  float* nrm3, uint8_t* img, uint8_t* rgb_img) {
+  GKvObjectCubeFloat cube;
+  if (!cube.create(Vector3i(dim[0], dim[1], dim[2]), Vector3f(origin[0], origin[1], origin[2]),
+                   Vector3f(center[0], center[1], center[2]), vox, true))
+    return 0;
+  const size_t n = (size_t)dim[0] * dim[1] * dim[2];
+  std::memcpy(cube.vp_tsdf(), tsdf, n * sizeof(float));
+  std::memcpy(cube.vp_w(), w, n);
+  std::memcpy(cube.vp_rgb(), rgb, 3 * n);
+  LGKvRendererTSDF r;
+  r.ip_Initialize_Parameters(&cube, W, H, K0[0], K0[1], K0[2], K0[3], mu, max_w);
+  const Vector3f c(cam[0], cam[1], cam[2]), li(light[0], light[1], light[2]);
+  if (variant == 0) {
+    r.rmis_Render_Maps_for_Scene(&cube, W, H, T_gc, T_cg, c, li, depth, vtx3, nrm3, img, rgb_img);
+  } else if (variant == 1) {
+    r.rmis_Render_Maps_for_Scene(&cube, W, H, T_gc, T_cg, c, li, depth, nrm3, img, rgb_img);
+  } else {
+    int lw = W, lh = H;
+    for (int l = 0; l < level; l++) lw /= 2, lh /= 2;
+    r.rmi_Render_Maps_for_ICP(&cube, lw, lh, T_gc, T_cg, c, li, level, depth, nrm3, img, rgb_img);
+  }
+  return 1;
+}
 #endif
 
 #if defined(REF_PIN_INTEG)
@@ -55,11 +86,12 @@ extern "C" int ref_render_icp(int W, int H, const float* K0, int level, const in
 
 // one cdtocc call on a cube given and returned in the reference layout (rgb:
 // three planes of the cube; img_rgb: three planes of the image, registered to
-// the depth image)
+// the depth image), then, where vol_valid (one byte per voxel) is given, one
+// uvv_Update_Valid_Volume carving over the sub-cubes this integration flagged
 extern "C" int ref_integrate_color(int W, int H, const float* K0, const int* dim, const float* origin,
                                    const float* center, float vox, float mu, float max_w, float* tsdf, uint8_t* w,
                                    uint8_t* rgb, const float* depth, const uint8_t* img_rgb, const float* T_gc,
-                                   const float* T_cg) {
+                                   const float* T_cg, const uint8_t* vol_valid) {
   GKvObjectCubeFloat cube;
   if (!cube.create(Vector3i(dim[0], dim[1], dim[2]), Vector3f(origin[0], origin[1], origin[2]),
                    Vector3f(center[0], center[1], center[2]), vox, true))
@@ -71,6 +103,13 @@ extern "C" int ref_integrate_color(int W, int H, const float* K0, const int* dim
   LGKvVolumeIntegrator integ;
   integ.ip_Initialize_Parameters(&cube, W, H, K0[0], K0[1], K0[2], K0[3], mu, max_w);
   integ.cdtocc_Convert_Depth_to_TSDF_on_Cube_with_Color(&cube, depth, img_rgb, W, H, T_gc, T_cg, true);
+  if (vol_valid) {
+    // carving over this integration's sub-cube flags (uvv_Update_Valid_Volume)
+    GKvVolumeBool vv;
+    vv.create(dim[0], dim[1], dim[2], 1, true);
+    for (size_t i = 0; i < n; i++) vv.vp()[i] = vol_valid[i] != 0;
+    integ.uvv_Update_Valid_Volume(&cube, &vv);
+  }
   std::memcpy(tsdf, cube.vp_tsdf(), n * sizeof(float));
   std::memcpy(w, cube.vp_w(), n);
   std::memcpy(rgb, cube.vp_rgb(), 3 * n);

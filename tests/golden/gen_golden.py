@@ -202,7 +202,7 @@ def refpin_gpu():
         Tgc = np.ascontiguousarray(gt[k], np.float32)
         Tcg = O.pose_inverse(Tgc)
         ri.ref_integrate_color(w, h, p(K0), p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(t), p(wt),
-                               p(col), p(np.ascontiguousarray(raw)), p(img), p(Tgc), p(np.ascontiguousarray(Tcg)))
+                               p(col), p(np.ascontiguousarray(raw)), p(img), p(Tgc), p(np.ascontiguousarray(Tcg)), None)
         depths.append(raw)
         imgs.append(img)
         tsdf.append(t.copy())
@@ -230,6 +230,26 @@ def refpin_gpu():
                      p(icp["T21"]), 0.01, p(ATA), p(ATb), p(ok))
     maps.update({"icp_depth": icp["depth"], "icp_T21": icp["T21"], "icp_K": K1, "icp_ATA": ATA, "icp_ATb": ATb,
                  "icp_ok": ok})
+    # the scene renders of the colour cube at pose 2
+    for var, (mode, level, has_v) in RENDER_VARIANTS.items():
+        lw, lh = w >> level, h >> level
+        d, v, nn, im, ci = (np.zeros(lw * lh, np.float32), np.zeros(3 * lw * lh, np.float32),
+                            np.zeros(3 * lw * lh, np.float32), np.zeros(lw * lh, np.uint8),
+                            np.zeros(3 * lw * lh, np.uint8))
+        rr.ref_render_variant(var, w, h, p(K0), level, p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(t),
+                              p(wt), p(col), p(Tgc), p(Tcg), p(cam), p(light), p(d), p(v), p(nn), p(im), p(ci))
+        maps.update({"var%d_depth" % var: d, "var%d_normal" % var: nn, "var%d_img" % var: im, "var%d_rgb" % var: ci})
+        if has_v:
+            maps["var%d_vertex" % var] = v
+    # a third integration (frame 2) followed by carving with carve_mask
+    raw = O.depth_to_m(depth_mm[2]).astype(np.float32)
+    raw[0, :] = raw[-1, :] = raw[:, 0] = raw[:, -1] = 0.0
+    img = np.ascontiguousarray(np.maximum(rgb[2], 1), np.uint8)
+    mask = carve_mask(dim)
+    ri.ref_integrate_color(w, h, p(K0), p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(t), p(wt), p(col),
+                           p(np.ascontiguousarray(raw)), p(img), p(Tgc), p(Tcg), p(mask))
+    maps.update({"carve_depth": raw, "carve_rgb": img, "carve_tsdf": t.copy(), "carve_weight": wt.copy(),
+                 "carve_colour": col.copy()})
     # the bilateral filter of the raw frame with holes of each kind
     bil = bilateral_input(O.depth_to_m(depth_mm[0]))
     out = np.zeros_like(bil)
@@ -239,6 +259,19 @@ def refpin_gpu():
                         cfg_origin=cfg["origin"], cfg_vox=vox, cfg_mu=0.03, cfg_maxw=100.0, depth=np.stack(depths),
                         rgb=np.stack(imgs), T=np.ascontiguousarray(gt[:3], np.float32), tsdf=np.stack(tsdf),
                         weight=np.stack(weight), colour=np.stack(colour), **maps)
+
+
+# the reference's other renders, by the index of ref_render_variant: the
+# oracle's mode bits (scene ray-cast 1, global normals 2, nearest-voxel colour
+# 4, white background 8), the pyramid level, and whether a vertex map is made
+RENDER_VARIANTS = {0: (1 | 2 | 4, 0, True), 1: (1 | 2, 0, False), 2: (2 | 8, 1, False)}
+
+
+def carve_mask(dim):
+    """valid voxels (one byte each, x fastest) of a slanted half-space
+    x + 2 y < 1.2 dim: sub-cubes past it are wholly invalid, those on it mixed"""
+    z, y, x = np.meshgrid(np.arange(dim), np.arange(dim), np.arange(dim), indexing="ij")
+    return np.ascontiguousarray((x + 2 * y < 1.2 * dim).reshape(-1).astype(np.uint8))
 
 
 def bilateral_input(depth):

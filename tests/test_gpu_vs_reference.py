@@ -4,7 +4,8 @@ tests/golden/refpin_gpu.npz holds what the reference's bilateral filter
 (d_bilateral_filter), integrator (g_fvsc + g_ctvc with colour) and renderer
 (g_rmi) computed, their sources run as host code (tests/golden/gen_golden.py).
 Here the sm_103a kernels take the same inputs through the C ABI and must give
-the same numbers: TSDF, weights, colour and the ray-cast maps bit for bit
+the same numbers: TSDF, weights, colour, carving and the ray-cast maps of all
+four renders bit for bit
 (FP32 TSDF storage, the reference's), the bilateral filter within 1e-5 m (the
 kernel uses the GPU's fast exponential where the host used expf) with the
 same holes.  tests/golden/refpin_track.npz holds the pose the reference's
@@ -83,6 +84,45 @@ def test_integration_and_raycast_against_the_reference_kernels(gpu):
             assert np.array_equal(_bits(gv.cpu().numpy()), _bits(g["vertex%d" % l])), l
             assert np.array_equal(_bits(gn.cpu().numpy()), _bits(g["normal%d" % l])), l
             assert np.array_equal(gi.cpu().numpy(), g["img%d" % l]), l
+        # the scene renders of the same cube (gen_golden.RENDER_VARIANTS)
+        for var, level, has_v in ((0, 0, True), (1, 0, False), (2, 1, False)):
+            lw, lh = s.levels[level][0], s.levels[level][1]
+            gd, gn = torch.zeros(lw * lh, dtype=torch.float32, device="cuda"), \
+                torch.zeros(3 * lw * lh, dtype=torch.float32, device="cuda")
+            gv = torch.zeros(3 * lw * lh, dtype=torch.float32, device="cuda") if has_v else None
+            gi, grgb = torch.zeros(lw * lh, dtype=torch.uint8, device="cuda"), \
+                torch.zeros(3 * lw * lh, dtype=torch.uint8, device="cuda")
+            if var == 2:
+                s.rmi_render_view(level, d_gc.data_ptr(), d_cg.data_ptr(), cam, light, gd.data_ptr(), gn.data_ptr(),
+                                  gi.data_ptr(), grgb.data_ptr())
+            else:
+                s.rmis_render_maps_for_scene(d_gc.data_ptr(), d_cg.data_ptr(), cam, light, gd.data_ptr(),
+                                             gv.data_ptr() if has_v else None, gn.data_ptr(), gi.data_ptr(),
+                                             grgb.data_ptr())
+            key = "var%d_" % var
+            assert np.array_equal(_bits(gd.cpu().numpy()), _bits(g[key + "depth"])), var
+            assert np.array_equal(_bits(gn.cpu().numpy()), _bits(g[key + "normal"])), var
+            assert np.array_equal(gi.cpu().numpy(), g[key + "img"]), var
+            if has_v:
+                assert np.array_equal(_bits(gv.cpu().numpy()), _bits(g[key + "vertex"])), var
+            rgb, rref = grgb.cpu().numpy().reshape(3, -1), g[key + "rgb"].reshape(3, -1)
+            # variant 0: the reference writes green into the red plane
+            # (z_yooji_cuda_tsdf_renderer.cu:185,1418); this library the true red
+            first = 1 if var == 0 else 0
+            assert np.array_equal(rgb[first:], rref[first:]), var
+        # a third integration, then carving of its wholly invalid sub-cubes
+        d_raw, d_rgb = _dev(g["carve_depth"]), _dev(g["carve_rgb"])
+        s.cdtocc_convert_depth_to_tsdf_color(d_raw.data_ptr(), d_rgb.data_ptr(), d_gc.data_ptr(), d_cg.data_ptr())
+        import sys
+        sys.path.insert(0, os.path.dirname(GOLD))
+        import gen_golden
+        assert s.uvv_update_valid_volume(gen_golden.carve_mask(int(g["cfg_dim"]))) > 20
+        t, w = s.volume()
+        assert np.array_equal(w, g["carve_weight"].astype(np.uint16))
+        m = w > 0
+        assert np.array_equal(_bits(t[m]), _bits(g["carve_tsdf"][m]))
+        assert (t[~m] == 1.0).all() and (g["carve_tsdf"][~m] == 1.0).all()
+        assert np.array_equal(s.color_volume().reshape(-1), g["carve_colour"])
 
 
 def test_tracking_against_the_reference_tracker(gpu):

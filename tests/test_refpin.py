@@ -207,6 +207,56 @@ def test_integration_and_raycast_match_the_reference_kernels_bit_for_bit(built):
         assert np.array_equal(img.reshape(-1), g["img%d" % l]), l
 
 
+def _check_variant(var, has_v, got, ref):
+    """got: the oracle's (depth, vertex, normals, image, colour); ref: the
+    reference's arrays.  Variant 0 (scene maps, nearest-voxel colour) keeps
+    the reference's red plane out of it: there the reference writes green
+    (z_yooji_cuda_tsdf_renderer.cu:185,1418), the oracle the true red"""
+    d, v, n, img, rgb = got
+    assert np.array_equal(_bits(d.reshape(-1)), _bits(ref["depth"])), var
+    assert np.array_equal(_bits(n.reshape(-1)), _bits(ref["normal"])), var
+    assert np.array_equal(img.reshape(-1), ref["img"]), var
+    if has_v:
+        assert np.array_equal(_bits(v.reshape(-1)), _bits(ref["vertex"])), var
+    rgb, rref = rgb.reshape(3, -1), ref["rgb"].reshape(3, -1)
+    if var == 0:
+        assert np.array_equal(rref[0], rref[1])
+        assert np.array_equal(rgb[1:], rref[1:])
+        assert (rgb[0] != rgb[1]).sum() > 0
+    else:
+        assert np.array_equal(rgb, rref), var
+
+
+def test_scene_renders_and_carving_match_the_reference_kernels_bit_for_bit(built):
+    """the oracle's three other renders against the reference's
+    rmis_Render_Maps_for_Scene (with and without a vertex map) and the
+    vertex-less rmi_Render_Maps_for_ICP, and its carving against
+    uvv_Update_Valid_Volume after a third integration"""
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import gen_golden
+    g = np.load(GOLD_GPU)
+    oc = _gpu_case_config(g)
+    vol = O.Volume(oc)
+    for k in range(2):
+        T = g["T"][k]
+        vol.integrate_color(g["depth"][k], g["rgb"][k], T, O.pose_inverse(T))
+    T = g["T"][2]
+    Ti, cam = O.pose_inverse(T), O.camera_center(T)
+    light = np.array([0, 0, -1], np.float32)
+    for var, (mode, level, has_v) in gen_golden.RENDER_VARIANTS.items():
+        got = vol.render_variant(mode, level, T, Ti, cam, light, vertex=has_v, color=True)
+        assert (got[0] > 0).sum() > 100
+        ref = {k: g["var%d_%s" % (var, k)] for k in ("depth", "normal", "img", "rgb") + (("vertex",) if has_v else ())}
+        _check_variant(var, has_v, got, ref)
+    vol.integrate_color(g["carve_depth"], g["carve_rgb"], T, Ti)
+    assert vol.update_valid_volume(gen_golden.carve_mask(int(g["cfg_dim"]))) > 20
+    t, w = vol.get()
+    assert np.array_equal(w, g["carve_weight"].astype(np.uint16))
+    assert np.array_equal(_bits(t), _bits(g["carve_tsdf"]))
+    assert np.array_equal(vol.get_color().reshape(-1), g["carve_colour"])
+
+
 def test_live_reference_kernels(built):
     """where the reference tree is mounted: a 160x120 sequence into a 96^3 cube,
     the oracle against the reference's renderer and integrator run live"""
@@ -230,6 +280,10 @@ def test_live_reference_kernels(built):
     n = dim ** 3
     t_ref, w_ref, c_ref = np.ones(n, np.float32), np.zeros(n, np.uint8), np.zeros(3 * n, np.uint8)
     vol = O.Volume(oc)
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import gen_golden
+    mask = gen_golden.carve_mask(dim)
     for k in range(3):
         raw = np.ascontiguousarray(O.depth_to_m(depth_mm[k]), np.float32)
         raw[0, :] = raw[-1, :] = raw[:, 0] = raw[:, -1] = 0.0
@@ -237,8 +291,10 @@ def test_live_reference_kernels(built):
         T = np.ascontiguousarray(gt[k], np.float32)
         Ti = np.ascontiguousarray(O.pose_inverse(T))
         vol.integrate_color(raw, img, T, Ti)
+        if k == 2:
+            assert vol.update_valid_volume(mask) > 100
         ri.ref_integrate_color(w, h, _p(K0), _p(dims), _p(org), _p(cen), oc.voxel_size, oc.mu, oc.max_w, _p(t_ref),
-                               _p(w_ref), _p(c_ref), _p(raw), _p(img), _p(T), _p(Ti))
+                               _p(w_ref), _p(c_ref), _p(raw), _p(img), _p(T), _p(Ti), _p(mask) if k == 2 else None)
         t, wt = vol.get()
         assert np.array_equal(wt, w_ref.astype(np.uint16)) and np.array_equal(_bits(t), _bits(t_ref)), k
         assert np.array_equal(vol.get_color().reshape(-1), c_ref), k
@@ -260,12 +316,24 @@ def test_live_reference_kernels(built):
             assert np.array_equal(_bits(a.reshape(-1)), _bits(b)), l
         assert np.array_equal(oi.reshape(-1), im), l
         if l == 0:
+            for var, (mode, vlev, has_v) in gen_golden.RENDER_VARIANTS.items():
+                vw, vh = w >> vlev, h >> vlev
+                ref = {"depth": np.zeros(vw * vh, np.float32), "vertex": np.zeros(3 * vw * vh, np.float32),
+                       "normal": np.zeros(3 * vw * vh, np.float32), "img": np.zeros(vw * vh, np.uint8),
+                       "rgb": np.zeros(3 * vw * vh, np.uint8)}
+                rr.ref_render_variant(var, w, h, _p(K0), vlev, _p(dims), _p(org), _p(cen), oc.voxel_size, oc.mu,
+                                      oc.max_w, _p(np.ascontiguousarray(t)), _p(wt.astype(np.uint8)), _p(c_ref), _p(T),
+                                      _p(Ti), _p(cam), _p(light), *(_p(ref[k]) for k in ("depth", "vertex", "normal",
+                                                                                          "img", "rgb")))
+                got = vol.render_variant(mode, vlev, T, Ti, cam, light, vertex=has_v, color=True)
+                assert (got[0] > 0).sum() > 300 >> (2 * vlev)
+                _check_variant(var, has_v, got, ref)
             # the per-pixel ICP term of the next frame against these maps
             icp = _icp_case(np.ascontiguousarray(O.depth_to_m(depth_mm[3]), np.float32))
             ATA, ATb, ok = np.zeros((w * h, 36), np.float32), np.zeros((w * h, 6), np.float32), np.zeros(w * h, np.uint8)
             rt.ref_icp_terms(w, h, _p(K0), _p(icp["depth"]), _p(d), _p(v), _p(nn), _p(icp["T21"]), 0.01, _p(ATA),
                              _p(ATb), _p(ok))
-            assert ok.sum() > 1000
+            assert ok.sum() > 200
             _check_icp_terms(w, h, K0, icp["depth"], v, nn, icp["T21"], ATA, ATb, ok)
 
 
