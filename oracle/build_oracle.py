@@ -9,6 +9,9 @@
 * oracle/_ref/libref_pin_{render,integ,track,imgproc}.so -- the reference's own
   renderer, integrator, tracker and bilateral-filter sources run as host code
   (see build_ref_pin_gpu), likewise only where the tree is present.
+* oracle/_ref/libref_pin_cpu.so -- the pyramid, point / normal map and
+  intrinsics functions of the reference's CPU image processor (see
+  build_ref_pin_cpu), likewise only where the tree is present.
 
 No -march flags: the same source must build on x86-64 and aarch64.
 -ffp-contract=off keeps GCC from fusing multiply-adds (the CUDA side builds
@@ -134,9 +137,109 @@ def build_ref_pin_gpu(force=False):
     return outs
 
 
+# member functions taken from the reference's CPU sources: (file, qualified
+# name, text that must follow the opening parenthesis, for overloads)
+_CPU_FUNCTIONS = [
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::set_from_params", ""),
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::get_params", ""),
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::back_project", "CKvPixel"),
+    ("Object/CPU/z_yooji_image_pyramid.cpp", "CKvYooji_Pyramid_Mat_Float::c_Create", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::cpm_Compute_Point_Map", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::enm_Estimate_Normal_Map", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::cpdd_Construct_Pyramids_Down_Depth", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::sdg5_Smooth_Depthmap_Gaussian_5x5", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::ddh_Downsample_Depthmap_Half", ""),
+    ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::dih_Downsample_Intrinsics_Half", ""),
+]
+
+
+def _skip_to(text, i, targets):
+    """index of the first character in `targets` at or after i outside
+    comments and string / character literals"""
+    n = len(text)
+    while i < n:
+        c = text[i]
+        if text.startswith("//", i):
+            i = text.find("\n", i)
+            i = n if i < 0 else i
+        elif text.startswith("/*", i):
+            i = text.find("*/", i + 2)
+            i = n if i < 0 else i + 2
+            continue
+        elif c in "\"'":
+            j = i + 1
+            while j < n and text[j] != c:
+                j += 2 if text[j] == "\\" else 1
+            i = j
+        elif c in targets:
+            return i
+        i += 1
+    raise ValueError("unbalanced source")
+
+
+def _function_text(text, qualname, after):
+    """the definition of qualname (return type to closing brace)"""
+    import re
+    pat = re.compile(r"(^|\n)([ \t]*[\w:<>\*& \t]+?\b)" + re.escape(qualname) + r"\s*\(\s*" + re.escape(after))
+    for m in pat.finditer(text):
+        start = m.start(2)
+        i = text.index("(", m.end(2) + len(qualname))
+        depth = 0
+        while True:  # the parameter list
+            i = _skip_to(text, i, "()")
+            depth += 1 if text[i] == "(" else -1
+            i += 1
+            if depth == 0:
+                break
+        j = _skip_to(text, i, "{;")
+        if text[j] == ";":
+            continue  # a declaration
+        depth = 0
+        while True:  # the body
+            j = _skip_to(text, j, "{}")
+            depth += 1 if text[j] == "{" else -1
+            j += 1
+            if depth == 0:
+                return text[start:j]
+    raise ValueError("%s not found" % qualname)
+
+
+def build_ref_pin_cpu(force=False):
+    """Member functions of the reference's CPU image processor, intrinsics and
+    pyramid classes, copied unchanged from the reference tree into
+    oracle/_ref/gen/cpu_functions.cpp and compiled with oracle/ref_pin_cpu.cpp
+    over the KAISION stand-ins.  Returns the path of libref_pin_cpu.so, or
+    None when the reference tree is absent."""
+    if not os.path.isdir(REF_STAC):
+        return None
+    out = os.path.join(HERE, "_ref", "libref_pin_cpu.so")
+    shim = os.path.join(HERE, "ref_shim", "cpu")
+    srcs = sorted({os.path.join(REF_STAC, f) for f, _, _ in _CPU_FUNCTIONS})
+    deps = srcs + [os.path.join(HERE, "ref_pin_cpu.cpp"), os.path.join(shim, "ref_kaision_shim.h")]
+    if not force and _newer(out, deps):
+        return out
+    gen = os.path.join(HERE, "_ref", "gen_cpu")
+    os.makedirs(gen, exist_ok=True)
+    texts = {}
+    parts = []
+    for f, name, after in _CPU_FUNCTIONS:
+        if f not in texts:
+            with open(os.path.join(REF_STAC, f), encoding="latin-1") as fh:
+                texts[f] = fh.read()
+        parts.append("// %s: %s\n%s\n" % (f, name, _function_text(texts[f], name, after)))
+    with open(os.path.join(gen, "cpu_functions.cpp"), "w", encoding="latin-1") as fh:
+        fh.write("\n".join(parts))
+    subprocess.check_call([CXX] + FLAGS + ["-fpermissive", "-w", "-I", shim, "-I", gen, "-o", out,
+                                           os.path.join(HERE, "ref_pin_cpu.cpp")])
+    os.remove(os.path.join(gen, "cpu_functions.cpp"))
+    os.rmdir(gen)
+    return out
+
+
 if __name__ == "__main__":
     force = "--force" in sys.argv
     print(build_oracle(force))
     print(build_ref_pin(force))
     print(build_ref_pin_cuda(force))
     print(build_ref_pin_gpu(force))
+    print(build_ref_pin_cpu(force))

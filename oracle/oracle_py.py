@@ -187,6 +187,30 @@ def load_ref_pin_gpu():
     return _ref_gpu
 
 
+_ref_cpu = None
+
+
+def load_ref_pin_cpu():
+    """The reference's CPU pyramid, point / normal map and intrinsics
+    functions: the library, or None when the reference tree is absent."""
+    global _ref_cpu
+    if _ref_cpu is None:
+        import build_oracle as _b
+        path = _b.build_ref_pin_cpu()
+        if path is None:
+            return None
+        lib = ctypes.CDLL(path)
+        P, I = ctypes.c_void_p, ctypes.c_int
+        lib.ref_depth_pyramid.restype = None
+        lib.ref_depth_pyramid.argtypes = [P, I, I, I, P]
+        lib.ref_point_normal_map.restype = None
+        lib.ref_point_normal_map.argtypes = [P, I, I, P, P, P]
+        lib.ref_level_intrinsics.restype = None
+        lib.ref_level_intrinsics.argtypes = [P, I, P]
+        _ref_cpu = lib
+    return _ref_cpu
+
+
 def config_from_vs(vs_cfg, reduce_mode=None, tsdf_store=None):
     """or_config equivalent to a vs_config (field by field)."""
     c = OrConfig()

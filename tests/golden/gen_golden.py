@@ -368,6 +368,51 @@ def refpin_track():
                         T_levels=T0, ok_init=ok1, T_init=T1)
 
 
+def cpu_case(w, h, seed):
+    """a bilateral-filtered depth frame (metres) with holes, zero lines and a
+    step, and level-0 intrinsics"""
+    import vs_scanner as V
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=1, seed=seed, dropout_iid=0.02)
+    d = V.synth_generate(sc)[0]
+    x = np.ascontiguousarray(O.bilateral(bilateral_input(O.depth_to_m(d[0]))), np.float32)
+    return x, np.array([f, f, w / 2.0, h / 2.0], np.float32)
+
+
+def ref_cpu_maps(lib, depth, K0, levels=3):
+    """the reference's depth pyramid, level intrinsics, and point / normal
+    maps of each level: (levels, K (levels x 4), vertices, normals)"""
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    h, w = depth.shape
+    sizes = [(w >> l, h >> l) for l in range(levels)]
+    flat = np.zeros(sum(a * b for a, b in sizes), np.float32)
+    lib.ref_depth_pyramid(p(depth), w, h, levels, p(flat))
+    Kl = np.zeros(4 * levels, np.float32)
+    lib.ref_level_intrinsics(p(K0), levels, p(Kl))
+    lv, vtx, nrm, off = [], [], [], 0
+    for l, (a, b) in enumerate(sizes):
+        lv.append(flat[off:off + a * b].reshape(b, a).copy())
+        off += a * b
+        v, n = np.zeros((b, a, 3), np.float32), np.zeros((b, a, 3), np.float32)
+        lib.ref_point_normal_map(p(lv[-1]), a, b, p(np.ascontiguousarray(Kl[4 * l:4 * l + 4])), p(v), p(n))
+        vtx.append(v)
+        nrm.append(n)
+    return lv, Kl.reshape(levels, 4), vtx, nrm
+
+
+def refpin_cpu():
+    """the reference's CPU image functions on a 90x66 frame (odd level sizes)"""
+    lib = O.load_ref_pin_cpu()
+    if lib is None:
+        raise SystemExit("the reference tree is not mounted; refpin_cpu.npz cannot be regenerated")
+    x, K0 = cpu_case(90, 66, seed=11)
+    lv, Kl, vtx, nrm = ref_cpu_maps(lib, x, K0)
+    out = {"depth0": x, "K0": K0, "K": Kl}
+    for l in range(3):
+        out.update({"pyr%d" % l: lv[l], "vertex%d" % l: vtx[l], "normal%d" % l: nrm[l]})
+    np.savez_compressed(os.path.join(OUT, "refpin_cpu.npz"), **out)
+
+
 def refpin_gpu_config(c):
     """or_config of the refpin_gpu case: float TSDF storage (the reference's)"""
     oc = O.OrConfig()
@@ -388,5 +433,6 @@ if __name__ == "__main__":
     refpin_cuda()
     refpin_gpu()
     refpin_track()
+    refpin_cpu()
     seq_small()
     print("fixtures written to", OUT)

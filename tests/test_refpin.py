@@ -462,3 +462,49 @@ def test_live_reference_tracker(built):
             assert np.array_equal(_bits(T), _bits(rT))
         else:
             assert np.array_equal(rT, gt[1])  # the reference leaves the pose
+
+
+# ---- the reference's CPU image processor (pyramid, point / normal maps) ------
+GOLD_CPU = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refpin_cpu.npz")
+
+
+def _check_cpu_maps(depth0, K0, ref_levels, ref_K, ref_vtx, ref_nrm):
+    """the oracle's pyramid (sdg5 + ddh), level intrinsics (dih) and point /
+    normal maps (cpm + enm, with the in-place rejection) against the
+    reference's"""
+    lib = O.load()
+    Kl = np.zeros(12, np.float32)
+    lib.or_level_intrinsics(_p(np.ascontiguousarray(K0, np.float32)), 3, _p(Kl))
+    assert np.array_equal(_bits(Kl), _bits(ref_K.reshape(-1)))
+    lv = [np.ascontiguousarray(depth0, np.float32)]
+    for l in range(1, 3):
+        lv.append(np.ascontiguousarray(O.pyramid_down(lv[-1]), np.float32))
+        assert np.array_equal(_bits(lv[l]), _bits(ref_levels[l])), l
+    for l in range(3):
+        v, n = O.point_normal_map(lv[l], Kl[4 * l:4 * l + 4].copy())
+        assert np.array_equal(_bits(v), _bits(ref_vtx[l])), l
+        assert np.array_equal(_bits(n), _bits(ref_nrm[l])), l
+    # the rejection recurrence is exercised: more invalid points than holes
+    assert (ref_vtx[0][..., 0] == -100).sum() > (lv[0] <= 0).sum()
+    assert (ref_nrm[0][..., 0] != -100).sum() > 300
+
+
+def test_pyramid_and_input_maps_match_the_reference_bit_for_bit(built):
+    """the reference's cpdd_Construct_Pyramids_Down_Depth, cpm_Compute_Point_Map,
+    enm_Estimate_Normal_Map and dih_Downsample_Intrinsics_Half
+    (z_yooji_image_processor.cpp:119-227,368-407,567-612,857-937), taken
+    unchanged from the reference tree over stand-ins for the KAISION types"""
+    g = np.load(GOLD_CPU)
+    _check_cpu_maps(g["depth0"], g["K0"], [g["pyr%d" % l] for l in range(3)], g["K"],
+                    [g["vertex%d" % l] for l in range(3)], [g["normal%d" % l] for l in range(3)])
+
+
+def test_live_reference_pyramid_and_input_maps(built):
+    """where the reference tree is mounted: ragged, QVGA and VGA frames"""
+    lib = O.load_ref_pin_cpu()
+    if lib is None:
+        pytest.skip("reference tree not mounted on this host")
+    G = _gen_golden()
+    for (w, h, seed) in ((97, 75, 3), (320, 240, 4), (640, 480, 5)):
+        x, K0 = G.cpu_case(w, h, seed)
+        _check_cpu_maps(x, K0, *G.ref_cpu_maps(lib, x, K0))
