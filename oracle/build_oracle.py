@@ -143,6 +143,12 @@ _CPU_FUNCTIONS = [
     ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::set_from_params", ""),
     ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::get_params", ""),
     ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::back_project", "CKvPixel"),
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::back_project", "CKvPointf"),
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Intrinsics::project", ""),
+    ("Object/CPU/z_yooji_camera_parameters.cpp", "CKvYooji_Extrinsics::transform", ""),
+    ("Object/CPU/z_yooji_matrix_rgbd.cpp", "CKvYooji_MatrixRgbD::convert_pixel_coord", ""),
+    ("Engine/CPU/z_yooji_object_scanner.cpp",
+     "CKvYooji_3D_Object_Scanner::z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates", ""),
     ("Object/CPU/z_yooji_image_pyramid.cpp", "CKvYooji_Pyramid_Mat_Float::c_Create", ""),
     ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::cpm_Compute_Point_Map", ""),
     ("Engine/CPU/z_yooji_image_processor.cpp", "LCKvYooji_Image_Processor::enm_Estimate_Normal_Map", ""),
@@ -215,7 +221,8 @@ def build_ref_pin_cpu(force=False):
     out = os.path.join(HERE, "_ref", "libref_pin_cpu.so")
     shim = os.path.join(HERE, "ref_shim", "cpu")
     srcs = sorted({os.path.join(REF_STAC, f) for f, _, _ in _CPU_FUNCTIONS})
-    deps = srcs + [os.path.join(HERE, "ref_pin_cpu.cpp"), os.path.join(shim, "ref_kaision_shim.h")]
+    deps = srcs + [os.path.join(HERE, "ref_pin_cpu.cpp"), os.path.join(shim, "ref_kaision_shim.h"),
+                   os.path.join(REF_UTIL, "_yooji_SITM_defines.h")]
     if not force and _newer(out, deps):
         return out
     gen = os.path.join(HERE, "_ref", "gen_cpu")
@@ -229,7 +236,7 @@ def build_ref_pin_cpu(force=False):
         parts.append("// %s: %s\n%s\n" % (f, name, _function_text(texts[f], name, after)))
     with open(os.path.join(gen, "cpu_functions.cpp"), "w", encoding="latin-1") as fh:
         fh.write("\n".join(parts))
-    subprocess.check_call([CXX] + FLAGS + ["-fpermissive", "-w", "-I", shim, "-I", gen, "-o", out,
+    subprocess.check_call([CXX] + FLAGS + ["-fpermissive", "-w", "-I", shim, "-I", gen, "-I", REF_UTIL, "-o", out,
                                            os.path.join(HERE, "ref_pin_cpu.cpp")])
     os.remove(os.path.join(gen, "cpu_functions.cpp"))
     os.rmdir(gen)

@@ -205,6 +205,8 @@ def load_ref_pin_cpu():
         lib.ref_depth_pyramid.argtypes = [P, I, I, I, P]
         lib.ref_point_normal_map.restype = None
         lib.ref_point_normal_map.argtypes = [P, I, I, P, P, P]
+        lib.ref_warp_depth.restype = None
+        lib.ref_warp_depth.argtypes = [P, I, I, P, P, P, I, I, P]
         lib.ref_level_intrinsics.restype = None
         lib.ref_level_intrinsics.argtypes = [P, I, P]
         _ref_cpu = lib

@@ -10,6 +10,7 @@
 //   cpdd_Construct_Pyramids_Down_Depth = sdg5 (5x5 Gaussian) + ddh (half)
 //   cpm_Compute_Point_Map + enm_Estimate_Normal_Map (half window 1)
 //   dih_Downsample_Intrinsics_Half
+//   z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates with convert_pixel_coord
 #include <cstdint>
 
 #include "ref_kaision_shim.h"
@@ -56,4 +57,22 @@ extern "C" void ref_level_intrinsics(const float* K0, int levels, float* Kl) {
     float dmin, dmax;
     in[l].get_params(Kl[4 * l], Kl[4 * l + 1], Kl[4 * l + 2], Kl[4 * l + 3], dmin, dmax);
   }
+}
+
+// the depth map seen from the colour camera: depth (wd x hd, metres) through
+// the depth intrinsics Kd, the depth-to-colour transform T (4x4 row-major)
+// and the colour intrinsics Kr into out (wr x hr), nearest depth kept
+extern "C" void ref_warp_depth(const float* depth, int wd, int hd, const float* Kd, const float* T, const float* Kr,
+                               int wr, int hr, float* out) {
+  CKvYooji_MatrixRgbD rig;
+  rig.zz_intrin_d.set_from_params(Kd[0], Kd[1], Kd[2], Kd[3]);
+  rig.zz_intrin_rgb.set_from_params(Kr[0], Kr[1], Kr[2], Kr[3]);
+  rig.zz_extrin_rgb_wrt_d.set_matrix(T);
+  rig.zz_image_rgb.c_Create(hr, wr);
+  CKvMatrixFloat d, o;
+  std::memcpy(d.c_Create(hd, wd)[0], depth, sizeof(float) * wd * hd);
+  o.c_Create(hr, wr);
+  CKvYooji_3D_Object_Scanner sc;
+  sc.z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates(&rig, &d, &o);
+  std::memcpy(out, o.vp(), sizeof(float) * wr * hr);
 }

@@ -2,7 +2,8 @@
 // processor is written on, and declarations of the reference classes whose
 // member functions oracle/build_oracle.py takes from the reference tree
 // (TEST INFRASTRUCTURE ONLY).  Only what those functions use is here, with the
-// semantics their call sites imply:
+// semantics their call sites imply (ROUNDF comes from the reference's own
+// STAC/Util/_yooji_SITM_defines.h):
 //   CKvMatrixFloat / CKvSet2d_of_Point3Df: a row-major matrix; ms(w, h) and
 //     mps(w, h) report width and height (mps also returns the row pointers),
 //     c_Create(rows, cols[, value]) sizes it (zero-filled without a value),
@@ -23,6 +24,7 @@ using std::sqrt;
 using std::vector;
 
 #define PI 3.14159265358979323846
+#include "_yooji_SITM_defines.h"
 
 struct CKvClass {};
 struct CKvPixel {
@@ -76,6 +78,7 @@ class KvMatrix {
 };
 typedef KvMatrix<float> CKvMatrixFloat;
 typedef KvMatrix<CKvPoint3Df> CKvSet2d_of_Point3Df;
+typedef KvMatrix<unsigned char> CKvMatrixUcharRgb;  // only its size is used
 
 // the reference's own classes (STAC/Object/CPU/_yooji_camera_parameters.h,
 // _yooji_image_pyramid.h, STAC/Engine/CPU/_yooji_image_processor.h), declared
@@ -87,11 +90,38 @@ class CKvYooji_Intrinsics : CKvClass {
                        float in_dmax = 100.0f);
   void get_params(float& in_fx, float& in_fy, float& in_px, float& in_py, float& in_dmin, float& in_dmax);
   void back_project(CKvPixel& in_xy, float in_Z, CKvPoint3Df& out_p3d);
+  void back_project(CKvPointf& in_xy, float in_Z, CKvPoint3Df& out_p3d);
+  bool project(CKvPoint3Df& in_p3d, CKvPointf& out_p);
 
  protected:
   CKvMatrixFloat zz_mat;
   float zz_fx = 0, zz_fy = 0, zz_px = 0, zz_py = 0;
   float zz_d_min = 0, zz_d_max = 0;
+};
+
+class CKvYooji_Extrinsics : CKvClass {
+ public:
+  CKvYooji_Extrinsics() { zz_mat.c_Create(4, 4, 0.0f); }
+  // the harness sets the 4x4 row-major transform directly
+  void set_matrix(const float* T) { std::memcpy(zz_mat.vp(), T, 16 * sizeof(float)); }
+  void transform(CKvPoint3Df& in_p3d, CKvPoint3Df& out_p);
+
+ protected:
+  CKvMatrixFloat zz_mat;
+};
+
+class CKvYooji_MatrixRgbD : public CKvClass {
+ public:
+  bool convert_pixel_coord(CKvPointf& in_point_depth, float in_depth, CKvPointf& out_point_rgb);
+  CKvYooji_Intrinsics zz_intrin_d, zz_intrin_rgb;
+  CKvYooji_Extrinsics zz_extrin_rgb_wrt_d;
+  CKvMatrixUcharRgb zz_image_rgb;
+};
+
+class CKvYooji_3D_Object_Scanner {
+ public:
+  void z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates(CKvYooji_MatrixRgbD* in_rgbd_img, CKvMatrixFloat* in_img_d,
+                                                         CKvMatrixFloat* out_img_d_transformed);
 };
 
 class CKvYooji_Pyramid_Mat_Float : public CKvClass {

@@ -410,7 +410,25 @@ def refpin_cpu():
     out = {"depth0": x, "K0": K0, "K": Kl}
     for l in range(3):
         out.update({"pyr%d" % l: lv[l], "vertex%d" % l: vtx[l], "normal%d" % l: nrm[l]})
+    # the same frame seen from a colour camera beside it (z_tdrcc)
+    T, Kr = warp_rig(90, 66)
+    warped = np.zeros((66, 90), np.float32)
+    p = lambda a: np.ascontiguousarray(a).ctypes.data_as(ctypes.c_void_p)
+    lib.ref_warp_depth(p(x), 90, 66, p(K0), p(T), p(Kr), 90, 66, p(warped))
+    out.update({"warp_T": T, "warp_Kr": Kr, "warp": warped})
     np.savez_compressed(os.path.join(OUT, "refpin_cpu.npz"), **out)
+
+
+def warp_rig(w, h):
+    """a colour camera 5 cm to the side, turned 3 degrees about y, with its
+    own intrinsics: (T depth -> colour 4x4, colour intrinsics)"""
+    a = np.deg2rad(3.0)
+    T = np.eye(4, dtype=np.float32)
+    T[0, 0] = T[2, 2] = np.cos(a)
+    T[0, 2], T[2, 0] = np.sin(a), -np.sin(a)
+    T[0, 3] = -0.05
+    f = 300.0 * w / 320.0
+    return T, np.array([f, 0.993 * f, w / 2.0 + 3.5, h / 2.0 - 1.75], np.float32)
 
 
 def refpin_gpu_config(c):

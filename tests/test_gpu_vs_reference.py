@@ -160,3 +160,16 @@ def test_tracking_against_the_reference_tracker(gpu):
         assert ok, key
         assert helpers.rot_err(T64, g[key]) < 1e-4, key
         assert helpers.trans_err(T64, g[key]) < 1e-4, key
+
+
+def test_registration_against_the_reference(gpu):
+    """the depth -> colour warp of tests/golden/refpin_cpu.npz (the reference's
+    z_tdrcc run on the host): bit for bit"""
+    torch = pytest.importorskip("torch")
+    g = np.load(os.path.join(os.path.dirname(GOLD), "refpin_cpu.npz"))
+    h, w = g["depth0"].shape
+    din = _dev(g["depth0"])
+    dout = torch.empty((h, w), dtype=torch.float32, device="cuda")
+    V.warp_depth_to_color(din.data_ptr(), w, h, g["K0"], g["warp_T"], g["warp_Kr"], w, h, dout.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(_bits(dout.cpu().numpy()), _bits(g["warp"]))

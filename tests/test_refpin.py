@@ -499,6 +499,17 @@ def test_pyramid_and_input_maps_match_the_reference_bit_for_bit(built):
                     [g["vertex%d" % l] for l in range(3)], [g["normal%d" % l] for l in range(3)])
 
 
+def test_registration_matches_the_reference_bit_for_bit(built):
+    """the oracle's depth -> colour warp against the reference's
+    z_tdrcc_Transform_Depth_to_Rgb_Camera_Coordinates (z_yooji_object_scanner.cpp:2429-2476)
+    with convert_pixel_coord (z_yooji_matrix_rgbd.cpp:101-118)"""
+    g = np.load(GOLD_CPU)
+    h, w = g["depth0"].shape
+    out = O.warp_depth(g["depth0"], g["K0"], g["warp_T"], g["warp_Kr"], w, h)
+    assert (g["warp"] > 0).mean() > 0.5
+    assert np.array_equal(_bits(out), _bits(g["warp"]))
+
+
 def test_live_reference_pyramid_and_input_maps(built):
     """where the reference tree is mounted: ragged, QVGA and VGA frames"""
     lib = O.load_ref_pin_cpu()
@@ -508,3 +519,10 @@ def test_live_reference_pyramid_and_input_maps(built):
     for (w, h, seed) in ((97, 75, 3), (320, 240, 4), (640, 480, 5)):
         x, K0 = G.cpu_case(w, h, seed)
         _check_cpu_maps(x, K0, *G.ref_cpu_maps(lib, x, K0))
+        # registration into a colour camera of the same size and of twice the size
+        T, Kr = G.warp_rig(w, h)
+        for (wr, hr, K) in ((w, h, Kr), (2 * w, 2 * h, Kr * np.float32(2))):
+            ref = np.zeros((hr, wr), np.float32)
+            lib.ref_warp_depth(_p(x), w, h, _p(K0), _p(T), _p(np.ascontiguousarray(K)), wr, hr, _p(ref))
+            assert (ref > 0).sum() > 0.2 * w * h
+            assert np.array_equal(_bits(O.warp_depth(x, K0, T, K, wr, hr)), _bits(ref)), (w, h, wr)
