@@ -526,6 +526,23 @@ def run_ours(args):
                         "event-timed duration; the ray-cast is issue-bound, not HBM-bound (see profiles/)" % n_stage,
                 "algorithmic_bytes_per_step": alg[dom] / n_stage,
                 "stages_gbs": achieved, "stages_frac": {k: v / peak for k, v in achieved.items()}}
+    if dom == "raycast":
+        # the ray-cast's own bound is instruction issue: warp instructions per
+        # ray from the committed ncu captures times this workload's rays, over
+        # the event-timed stage, against one warp instruction per scheduler per
+        # cycle (4 per SM) at the SM clock sampled during the timed region
+        ia = traffic_per_unit("k_ray_march", "warp_inst_per_ray")
+        ib = traffic_per_unit("k_ray_shade", "warp_inst_per_ray")
+        mhz = (clocks or {}).get("sm_mhz")
+        if ia is not None and ib is not None and mhz:
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            got = (ia + ib) * rays / (stage_sum[dom_i] / n_stage * 1e-3)
+            top = 4.0 * sms * mhz * 1e6
+            roofline["issue"] = {"achieved": got, "peak": top, "unit": "warp instructions/s", "frac": got / top,
+                                 "warp_inst_per_ray": ia + ib,
+                                 "note": "warp instructions per ray from profiles/ncu_traffic.txt x %.0f rays per "
+                                         "step / the stage's event time; peak = 4 x %d SMs x %.0f MHz" %
+                                         (rays, sms, mhz)}
 
     cpu = None
     ate = None
