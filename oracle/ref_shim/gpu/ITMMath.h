@@ -50,11 +50,13 @@ struct Vector3_ {
     x /= s, y /= s, z /= s;
     return *this;
   }
-  // integer part by truncation and the remainder (the reference's CPU twin
-  // of the trilinear read, z_yooji_cube_tsdf_float.cpp:376-378, truncates;
-  // for the non-negative coordinates inside a cube this is the floor)
+  // the floor and the remainder v - floor(v), the InfiniTAM convention the
+  // oracle restates (the reference's CPU twin of the trilinear read,
+  // z_yooji_cube_tsdf_float.cpp:376-378, truncates instead; the two differ
+  // only for a coordinate in (-1, 0), where the floor's tap at -1 makes the
+  // read invalid)
   Vector3_<int> toInt(Vector3_<float>& residual) const {
-    const Vector3_<int> i((int)x, (int)y, (int)z);
+    const Vector3_<int> i((int)std::floor(x), (int)std::floor(y), (int)std::floor(z));
     residual = Vector3_<float>((float)(x - (T)i.x), (float)(y - (T)i.y), (float)(z - (T)i.z));
     return i;
   }

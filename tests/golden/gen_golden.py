@@ -431,6 +431,94 @@ def warp_rig(w, h):
     return T, np.array([f, 0.993 * f, w / 2.0 + 3.5, h / 2.0 - 1.75], np.float32)
 
 
+def pipeline_case(w=120, h=90, dim=96, size=0.75, frames=4, seed=7):
+    """a depth sequence and the or_config of the reference's settings for the
+    whole per-frame path (float TSDF, block-tree reduction, ICP {10, 7, 7},
+    distance (0.055 size)^2, no normal test)"""
+    import vs_scanner as V
+    f = 285.0 * w / 320.0
+    sc = V.synth_config(w, h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, n_frames=frames, seed=seed, dropout_iid=0.01)
+    dmm, gt, centre = V.synth_generate(sc)
+    origin, vox = V.cube_around(centre, size, dim)
+    oc = refpin_gpu_config(dict(width=w, height=h, fx=f, fy=f, cx=w / 2.0, cy=h / 2.0, dim=dim,
+                                origin=np.array(origin, np.float32), voxel_size=vox, mu=0.03, max_w=100.0))
+    oc.reduce_mode = 0
+    oc.th_icp = float(np.float32((0.055 * size) ** 2))
+    for k, n in enumerate((10, 7, 7)):
+        oc.icp_iters[k] = n
+    return oc, dmm
+
+
+def ref_pipeline(oc, dmm):
+    """the per-frame path chained from the reference's own stages, in the
+    order of its scanner loop (z_yooji_object_scanner.cpp: z_uid bilateral,
+    z_cip pyramid, z_ecp track from the second frame, z_uom integrate the raw
+    depth, z_uts ray-cast every level): bilateral (d_bilateral_filter),
+    pyramid (cpdd), tp_Track_Pose, cdtocc, rmi_Render_Maps_for_ICP, with the
+    reference's inverse (d_im_Inverse_Matrix_4x4) and camera centre (d_gcc).
+    Returns (per-frame poses, tracked flags, tsdf, weights, model depth /
+    vertex / normal of each level after the last frame)."""
+    rr, ri, rt, rb = O.load_ref_pin_gpu()
+    cpu, m4, cu = O.load_ref_pin_cpu(), O.load_ref_pin(), O.load_ref_pin_cuda()
+    p = lambda a: np.ascontiguousarray(a).ctypes.data_as(ctypes.c_void_p)
+    w, h, dim = oc.width, oc.height, oc.dim[0]
+    geo = np.zeros(5, np.float32)
+    O.load().or_config_geometry(ctypes.byref(oc), p(geo))
+    K0 = np.array([oc.fx, oc.fy, oc.cx, oc.cy], np.float32)
+    dims, org, cen = np.array([dim] * 3, np.int32), np.array(list(oc.origin), np.float32), np.ascontiguousarray(geo[:3])
+    n = dim ** 3
+    tsdf, wt, col = np.ones(n, np.float32), np.zeros(n, np.uint8), np.zeros(3 * n, np.uint8)
+    rgb = np.full((3, h, w), 128, np.uint8)
+    sizes = [(w >> l, h >> l) for l in range(3)]
+    T = np.eye(4, dtype=np.float32)
+    md = [np.zeros(a * b, np.float32) for a, b in sizes]
+    mv = [np.zeros(3 * a * b, np.float32) for a, b in sizes]
+    mn = [np.zeros(3 * a * b, np.float32) for a, b in sizes]
+    poses, tracked = [], []
+    for k in range(dmm.shape[0]):
+        raw = np.ascontiguousarray(dmm[k].astype(np.float32) * np.float32(oc.depth_scale))
+        filt = np.zeros_like(raw)
+        rb.ref_bilateral(w, h, p(raw), p(filt))
+        flat = np.zeros(sum(a * b for a, b in sizes), np.float32)
+        cpu.ref_depth_pyramid(p(filt), w, h, 3, p(flat))
+        lv, off = [], 0
+        for a, b in sizes:
+            lv.append(np.ascontiguousarray(flat[off:off + a * b]))
+            off += a * b
+        ok = 1
+        if k > 0:
+            ok, Tn = ref_track(rt, oc, lv, md, mv, mn, T, None)
+            if ok:
+                T = np.ascontiguousarray(Tn, np.float32)
+        poses.append(T.copy())
+        tracked.append(int(ok))
+        if not ok:
+            continue
+        Ti = np.zeros(16, np.float32)
+        m4.ref_inverse4(p(T), p(Ti))
+        cam = np.zeros(3, np.float32)
+        cu.ref_camera_center(p(T), p(cam))
+        ri.ref_integrate_color(w, h, p(K0), p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(tsdf), p(wt),
+                               p(col), p(raw), p(rgb), p(T), p(Ti), None)
+        for l, (a, b) in enumerate(sizes):
+            img = np.zeros(a * b, np.uint8)
+            rr.ref_render_icp(w, h, p(K0), l, p(dims), p(org), p(cen), oc.voxel_size, oc.mu, oc.max_w, p(tsdf),
+                              p(wt), p(T), p(Ti), p(cam), p(np.array([0, 0, -1], np.float32)), p(md[l]), p(mv[l]),
+                              p(mn[l]), p(img))
+    return np.stack(poses), np.array(tracked, np.int32), tsdf, wt, md, mv, mn
+
+
+def refpin_pipeline():
+    """four 120x90 frames through the reference's own stages (about a minute:
+    the tracker's block trees run as cooperative threads)"""
+    if O.load_ref_pin_gpu() is None or O.load_ref_pin_cpu() is None:
+        raise SystemExit("the reference tree is not mounted; refpin_pipeline.npz cannot be regenerated")
+    oc, dmm = pipeline_case()
+    poses, tracked, tsdf, wt, md, mv, mn = ref_pipeline(oc, dmm)
+    np.savez_compressed(os.path.join(OUT, "refpin_pipeline.npz"), depth_mm=dmm, poses=poses, tracked=tracked,
+                        weight=wt, depth0=md[0], vertex0=mv[0], normal0=mn[0])
+
+
 def refpin_gpu_config(c):
     """or_config of the refpin_gpu case: float TSDF storage (the reference's)"""
     oc = O.OrConfig()
@@ -452,5 +540,6 @@ if __name__ == "__main__":
     refpin_gpu()
     refpin_track()
     refpin_cpu()
+    refpin_pipeline()
     seq_small()
     print("fixtures written to", OUT)

@@ -526,3 +526,46 @@ def test_live_reference_pyramid_and_input_maps(built):
             lib.ref_warp_depth(_p(x), w, h, _p(K0), _p(T), _p(np.ascontiguousarray(K)), wr, hr, _p(ref))
             assert (ref > 0).sum() > 0.2 * w * h
             assert np.array_equal(_bits(O.warp_depth(x, K0, T, K, wr, hr)), _bits(ref)), (w, h, wr)
+
+
+# ---- the whole per-frame path, chained from the reference's own stages -------
+GOLD_PIPE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "refpin_pipeline.npz")
+
+
+def _check_pipeline(oc, dmm, poses, tracked, weight, depth0, vertex0, normal0):
+    s = O.Session(oc)
+    for k in range(dmm.shape[0]):
+        assert s.frame(dmm[k]) == bool(tracked[k]), k
+        assert np.array_equal(_bits(s.pose()), _bits(poses[k])), k
+    _, w = s.volume().get()
+    assert np.array_equal(w, weight.astype(np.uint16))
+    m = s.maps(0)
+    assert (depth0 > 0).sum() > 1000
+    assert np.array_equal(_bits(m["model_depth"]), _bits(depth0.reshape(m["model_depth"].shape)))
+    assert np.array_equal(_bits(m["model_vertex"]), _bits(vertex0.reshape(m["model_vertex"].shape)))
+    assert np.array_equal(_bits(m["model_normal"]), _bits(normal0.reshape(m["model_normal"].shape)))
+
+
+def test_whole_frame_loop_matches_the_reference_stages_bit_for_bit(built):
+    """four frames through the oracle's session (its own stage order) against
+    the same frames through the reference's own bilateral filter, pyramid,
+    tracker, integrator and renderer chained in the reference scanner's order:
+    every pose, the tracked flags, the final weights and the final level-0
+    model maps are identical"""
+    g = np.load(GOLD_PIPE)
+    oc, dmm = _gen_golden().pipeline_case()
+    assert np.array_equal(dmm, g["depth_mm"])
+    assert g["tracked"].all()
+    _check_pipeline(oc, dmm, g["poses"], g["tracked"], g["weight"], g["depth0"], g["vertex0"], g["normal0"])
+
+
+def test_live_whole_frame_loop(built):
+    """where the reference tree is mounted: three 80x60 frames into a 64^3
+    cube, a case whose rays sample within one voxel of the cube's low faces
+    (where ITMMath's toInt decides the trilinear taps)"""
+    if O.load_ref_pin_gpu() is None or O.load_ref_pin_cpu() is None:
+        pytest.skip("reference tree not mounted on this host")
+    G = _gen_golden()
+    oc, dmm = G.pipeline_case(w=80, h=60, dim=64, frames=3, seed=8)
+    poses, tracked, tsdf, wt, md, mv, mn = G.ref_pipeline(oc, dmm)
+    _check_pipeline(oc, dmm, poses, tracked, wt, md[0], mv[0], mn[0])
