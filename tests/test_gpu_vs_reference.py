@@ -173,3 +173,36 @@ def test_registration_against_the_reference(gpu):
     V.warp_depth_to_color(din.data_ptr(), w, h, g["K0"], g["warp_T"], g["warp_Kr"], w, h, dout.data_ptr())
     torch.cuda.synchronize()
     assert np.array_equal(_bits(dout.cpu().numpy()), _bits(g["warp"]))
+
+
+def test_whole_frame_loop_against_the_reference_stages(gpu):
+    """tests/golden/refpin_pipeline.npz: four frames through the reference's
+    own stages in its scanner's order.  The CUDA session with the reference's
+    settings (FP32 TSDF, iterations {10, 7, 7}, distance (0.055 size)^2, no
+    normal test) tracks every frame, each pose within 1e-4 rad / 1e-4 m of the
+    reference's, and its final level-0 model depth agrees on 99.9 % of the
+    pixels within 1 mm"""
+    import sys
+    import helpers
+    g = np.load(os.path.join(os.path.dirname(GOLD), "refpin_pipeline.npz"))
+    d = os.path.dirname(GOLD)
+    if d not in sys.path:
+        sys.path.insert(0, d)
+    import gen_golden
+    oc, dmm = gen_golden.pipeline_case()
+    assert np.array_equal(dmm, g["depth_mm"])
+    cfg = V.default_config(oc.width, oc.height, fx=oc.fx, fy=oc.fy, cx=oc.cx, cy=oc.cy, dim=tuple(oc.dim),
+                           origin=list(oc.origin), voxel_size=oc.voxel_size, mu=oc.mu, max_w=oc.max_w,
+                           th_icp=oc.th_icp, cos_normal=-3.0, icp_iters=(10, 7, 7), tsdf_type=V.VS_TSDF_FP32,
+                           reduce_mode=V.VS_REDUCE_FP64)
+    with V.Session(cfg) as s:
+        for k in range(dmm.shape[0]):
+            T, tracked = s.scan_frame_host(dmm[k])
+            assert tracked == bool(g["tracked"][k]), k
+            assert helpers.rot_err(T, g["poses"][k]) < 1e-4, k
+            assert helpers.trans_err(T, g["poses"][k]) < 1e-4, k
+        md = s.maps(0)["model_depth"].reshape(-1)
+    rd = g["depth0"].reshape(-1)
+    both = (md > 0) & (rd > 0)
+    assert ((md > 0) == (rd > 0)).mean() > 0.999
+    assert (np.abs(md[both] - rd[both]) < 1e-3).mean() > 0.999
