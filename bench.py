@@ -112,12 +112,20 @@ def generate(spec):
     return depth, gt, centre
 
 
+def session_mu(vox):
+    """truncation of a session: 2 cm, or 5 voxels where that is more (the
+    reference's own rule is 5 voxels, VCL_Volume_Scanner_View.cpp:423; at
+    1.7 voxels, 2 cm in a 128^3 volume over 1.5 m, the ray-cast misses most of
+    the thin first-frame band and tracking fails, in the oracle as here)"""
+    return max(MIX["mu"], 5.0 * float(vox))
+
+
 def make_config(spec, centre):
     import vs_scanner as V
 
     origin, vox = V.cube_around(centre, MIX["size_m"], spec["dim"])
     return V.default_config(spec["w"], spec["h"], fx=spec["f"], fy=spec["f"], cx=spec["cx"], cy=spec["cy"],
-                            dim=(spec["dim"],) * 3, origin=origin, voxel_size=vox, mu=MIX["mu"],
+                            dim=(spec["dim"],) * 3, origin=origin, voxel_size=vox, mu=session_mu(vox),
                             th_icp=MIX["th_icp"], cos_normal=float(np.cos(np.radians(MIX["normal_deg"]))),
                             icp_iters=MIX["icp_iters"], tsdf_type=V.VS_TSDF_INT16, reduce_mode=V.VS_REDUCE_KAHAN)
 

@@ -48,3 +48,81 @@ def camera_centre_err(A, B):
 def q16(t):
     """int16 quantisation of a TSDF array (the product's storage)"""
     return np.clip(np.rint(np.asarray(t, np.float32) * np.float32(32767.0)), -32767, 32767).astype(np.int32)
+
+
+ONE_INT16_STEP = 1.0 / 32767.0
+
+
+def assert_tsdf_within_one_step(t, ref):
+    """TSDF contract: within one int16 quantisation step of the reference's
+    value (float storages; int16 storage compares the quantised codes)"""
+    d = np.abs(np.asarray(t, np.float64) - np.asarray(ref, np.float64))
+    assert d.size and d.max() <= ONE_INT16_STEP * (1.0 + 1e-6), d.max()
+
+
+def assert_maps_match(depth, vtx, nrm, img, rdepth, rvtx, rnrm, rimg, what=""):
+    """Ray-cast contract: the hit masks agree on >= 99.9 % of the pixels, and
+    where both hit, vertices and depth within 1 mm on >= 99.9 % of them; the
+    normals and the shaded image follow the surface point (normals within
+    1e-2, image within 2 levels, on >= 99.9 %)."""
+    depth, rdepth = np.asarray(depth).reshape(-1), np.asarray(rdepth).reshape(-1)
+    hit, rhit = depth > 0, rdepth > 0
+    assert (hit == rhit).mean() >= 0.999, (what, (hit == rhit).mean())
+    both = hit & rhit
+    assert both.sum() > 0, what
+    v, rv = np.asarray(vtx).reshape(-1, 3)[both], np.asarray(rvtx).reshape(-1, 3)[both]
+    assert (np.linalg.norm(v - rv, axis=1) <= 1e-3).mean() >= 0.999, what
+    assert (np.abs(depth[both] - rdepth[both]) <= 1e-3).mean() >= 0.999, what
+    if nrm is not None:
+        n, rn = np.asarray(nrm).reshape(-1, 3)[both], np.asarray(rnrm).reshape(-1, 3)[both]
+        assert (np.abs(n - rn).max(axis=1) <= 1e-2).mean() >= 0.999, what
+    if img is not None:
+        i, ri = np.asarray(img).reshape(-1)[both].astype(int), np.asarray(rimg).reshape(-1)[both].astype(int)
+        assert (np.abs(i - ri) <= 2).mean() >= 0.999, what
+
+
+def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_poses=True):
+    """Runs `frames` frames stage by stage through a session and hands the
+    session's own tracking inputs (model maps of the previous ray-cast,
+    filtered input pyramid, input normals, previous pose) to the oracle's
+    tracker at every frame: the tracked flag must equal the FP32 oracle's,
+    and where both track, the pose must be within 1e-4 rad and 0.1 mm of the
+    FP32 and FP64 oracles' (the per-frame tolerance on identical inputs).
+    Returns the largest rotation (rad) and translation (m) differences and
+    the frames lost."""
+    import torch
+
+    ocfg = O.config_from_vs(cfg)
+    worst = [0.0, 0.0]
+    lost = []
+    with V.Session(cfg) as s:
+        for k in range(frames):
+            T_prev, T_prev64, _ = s.pose()
+            mv = [s.maps(l)["model_vertex"] for l in range(cfg.levels)]
+            mn = [s.maps(l)["model_normal"] for l in range(cfg.levels)]
+            d = torch.from_numpy(np.ascontiguousarray(depth[k]).view(np.int16)).cuda()
+            s.stage_filter(d.data_ptr())
+            s.stage_track()
+            T, T64, info = s.pose()
+            if k > 0:
+                m = [s.maps(l) for l in range(cfg.levels)]
+                ind = [x["input_depth"] for x in m]
+                inn = [x["input_normal"] for x in m] if cfg.cos_normal > -2.0 else None
+                ok32, oT, _ = O.track(ocfg, ind, mv, mn, T_prev, innrm_levels=inn, f64=False)
+                ok64, dT, _ = O.track(ocfg, ind, mv, mn, T_prev64, innrm_levels=inn, f64=True)
+                assert bool(info[0]) == ok32, (k, info[0], ok32)
+                if expect_tracked:
+                    assert ok32 and ok64, (k, ok32, ok64)
+                if not info[0]:
+                    lost.append(k)
+                    assert np.array_equal(T64, T_prev64), k  # a lost frame leaves the pose
+                if compare_poses and info[0] and ok64:
+                    for ref in (oT, dT):
+                        r, t = rot_err(T64, ref), trans_err(T64, ref)
+                        worst[0], worst[1] = max(worst[0], r), max(worst[1], t)
+                        assert r < 1e-4 and t < 1e-4, (k, r, t)
+            s.stage_integrate()
+            s.stage_raycast()
+            s.sync()
+        final = dict(pose=s.pose()[0], volume=s.volume(), maps=[s.maps(l) for l in range(cfg.levels)])
+    return worst, lost, final

@@ -161,7 +161,10 @@ def _compare(od, ov, on, oi, orgb, gd, gv, gn, gi, grgb):
     assert np.percentile(np.abs(gn[both] - on[both]).max(1), 99.9) < 1e-3
     assert (np.abs(gi[same].astype(int) - oi[same].astype(int)) <= 1).mean() >= 0.999
     if orgb is not None:
-        assert (grgb[:, same] == orgb[:, same]).all()
+        # colour of a surface point within the ray-cast tolerance: within one
+        # level on 99.9 % of the pixels
+        dc = np.abs(grgb.astype(np.int32) - orgb.astype(np.int32))[:, same]
+        assert (dc.max(axis=0) <= 1).mean() >= 0.999
 
 
 @pytest.mark.gpu

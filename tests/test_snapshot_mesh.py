@@ -68,6 +68,10 @@ def test_mesh_matches_oracle(gpu, case):
             vol.integrate(raw, Tgc, Tcg)
             d = [torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in (raw, Tgc, Tcg)]
             s.cdtoc_convert_depth_to_tsdf(d[0].data_ptr(), d[1].data_ptr(), d[2].data_ptr())
+        # the extraction compared on the identical volume (integration parity
+        # is within one int16 step, tested on its own)
+        t, w = vol.get()
+        s.set_volume(t, w)
         gxyz, _ = s.mesh()
     oxyz, _ = vol.mesh()
     assert len(oxyz) > 1000

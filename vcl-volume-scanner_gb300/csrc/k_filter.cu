@@ -53,7 +53,8 @@ __device__ inline float bilateral_px(const BilateralSmem& m, int tx, int ty, con
 template <bool FROM_MM>
 __device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restrict__ mm,
                                       const float* __restrict__ fin, float scale, float* __restrict__ raw_out,
-                                      float* __restrict__ out, int W, int H, int x0, int y0, const float g[5]) {
+                                      float* __restrict__ out, int W, int H, int x0, int y0, const float g[5],
+                                      float2* __restrict__ dl_out = nullptr, const float* __restrict__ lam = nullptr) {
   const int tid = threadIdx.y * BX + threadIdx.x;
   for (int i = tid; i < (BY + 5) * (BX + 5); i += BX * BY) {
     int ty = i / (BX + 5), tx = i - ty * (BX + 5);
@@ -75,7 +76,11 @@ __device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restri
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int x = x0 + tx, y = y0 + ty;
   if (x < W && y < H) {
-    if (FROM_MM) raw_out[(size_t)y * W + x] = m.tex[ty + 3][tx + 3];
+    if (FROM_MM) {
+      const float raw = m.tex[ty + 3][tx + 3];
+      raw_out[(size_t)y * W + x] = raw;
+      if (dl_out) dl_out[(size_t)y * W + x] = make_float2(raw, __ldg(lam + (size_t)y * W + x));
+    }
     out[(size_t)y * W + x] = bilateral_px(m, tx, ty, g);
   }
 }
@@ -92,7 +97,7 @@ __global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __
     const int tw = (W + BX - 1) / BX;
     const float g[5] = {s->gauss[0], s->gauss[1], s->gauss[2], s->gauss[1], s->gauss[0]};
     bilateral_tile<true>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
-                         (t / tw) * BY, g);
+                         (t / tw) * BY, g, s->lam_map ? s->dl_map : nullptr, s->lam_map);
     if (s->rgb_packed) {
       // the colour frame as one word per pixel, for the integration's gathers
       const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * BY + threadIdx.y;

@@ -122,8 +122,11 @@ __global__ void __launch_bounds__(256) k_activate(const BatchTable* __restrict__
       int b = (zs * nb1 + ys) * nb0 + xs;
       if (b == prev) continue;
       prev = b;
+      // an L1-cached read of the flag may be stale, but only ever with an
+      // older stamp, and the exchange then decides: it returns the current
+      // stamp to every thread but the first
       uint32_t* f = s->brick_flag + b;
-      if (*((volatile uint32_t*)f) != stamp && atomicExch(f, stamp) != stamp) {
+      if (*f != stamp && atomicExch(f, stamp) != stamp) {
         uint32_t pos = atomicAdd(s->brick_count, 1u);
         s->brick_list[pos] = (uint32_t)b;
       }
@@ -190,6 +193,46 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.d1 = s->dim[1];
 }
 
+// the values of the per-voxel loop of the update kernel
+struct VoxParams {
+  // depth source: the session's packed {depth, lambda^-1} map (packed), or
+  // a depth map with the lambda^-1 map beside it (lam) or without (NULL:
+  // computed per voxel from the ray table)
+  const void* src;
+  const float* lam;
+  float K[4];
+  float mu, inv_mu, max_w;
+  int W, H;
+  bool packed;
+  bool fast;  // principal point within the bound of nearest_pixel's fast path
+};
+
+__device__ inline void load_vox_params(VoxParams& p, const SessionDev* __restrict__ s, const float* depth_ext) {
+  p.packed = !depth_ext && s->dl_map;
+  p.src = p.packed ? static_cast<const void*>(s->dl_map) : static_cast<const void*>(depth_ext ? depth_ext : s->depth_raw);
+  p.lam = p.packed ? nullptr : s->lam_map;
+#pragma unroll
+  for (int k = 0; k < 4; k++) p.K[k] = s->lv[0].K[k];
+  p.mu = s->mu;
+  p.inv_mu = 1.0f / s->mu;
+  p.max_w = s->max_w;
+  p.W = s->lv[0].W;
+  p.H = s->lv[0].H;
+  p.fast = fabsf(p.K[2]) < 4096.0f && fabsf(p.K[3]) < 4096.0f;
+}
+
+// A load the compiler may neither hoist out of the brick loop nor keep in a
+// register across it: the session's brick-level values are read again at each
+// brick (L1 hits), so they take no registers while the voxels are processed.
+template <class T>
+__device__ __forceinline__ T reload(const T* p) {
+  return *reinterpret_cast<const volatile T*>(p);
+}
+template <class T>
+__device__ __forceinline__ T* reload(T* const* p) {
+  return *reinterpret_cast<T* const volatile*>(p);
+}
+
 // The colour part of g_ctvc (z_yooji_cuda_volume_integrator.cu:404-455, the
 // registered-colour path): for every voxel of the round whose depth was just
 // updated, the colour at its projection, interpolated as
@@ -219,13 +262,15 @@ __device__ inline bool interp_channel(uint32_t a, uint32_t b, uint32_t c, uint32
   return true;
 }
 
-template <class S, int kPerVec, class IP, class WV>
+// wv: the round's words, [vector][voxel in vector]; v0: the lane's index of
+// the round's first voxel
+template <class S, int kPerVec, int kRound, class IP, class WV>
 __device__ void color_round(const IP& q, unsigned upd, int v0, int lane, int bx, int by, int bz, uint32_t b,
                             const WV& wv, const float* __restrict__ lx, const float* __restrict__ ly,
                             const float* __restrict__ lz) {
   constexpr int kG = 4;
 #pragma unroll
-  for (int g = 0; g < 8; g += kG) {
+  for (int g = 0; g < kRound; g += kG) {
     uint32_t t00[kG], t01[kG], t10[kG], t11[kG], oc[kG];
     float rxs[kG], rys[kG];
     bool ok[kG];
@@ -258,7 +303,7 @@ __device__ void color_round(const IP& q, unsigned upd, int v0, int lane, int bx,
       const int li = (k * 32 + lane) * kPerVec + e;
       float tn;
       uint32_t wn;
-      S::decode(wv[k][e], tn, wn);  // the updated word: weight w + 1
+      S::decode(wv[(g + j) / kPerVec][e], tn, wn);  // the updated word: weight w + 1
       const float oldW = (float)(wn - 1u), inewW = __ldg(g_inv_weight + wn);
       float smp[3];
       bool good = true;
@@ -275,14 +320,78 @@ __device__ void color_round(const IP& q, unsigned upd, int v0, int lane, int bx,
 }
 
 #ifndef VS_INT_MIN_BLOCKS
-#define VS_INT_MIN_BLOCKS 2  // resident 256-thread blocks per SM the register allocation must allow
+#define VS_INT_MIN_BLOCKS 4  // resident 256-thread blocks per SM the register allocation must allow
 #endif
 
+// rcp.approx.ftz.f32: the reciprocal with at most 1 ulp of error (PTX ISA,
+// "rcp.approx"), one special-function instruction
+__device__ __forceinline__ float rcp_approx(float z) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(z));
+  return r;
+}
+
+// Nearest pixel of a camera-frame point: (__float2int_rn(u), __float2int_rn(v))
+// of d_p_Project's u = K0 x / z + K2, v = K1 y / z + K3 with IEEE division
+// (_yooji_cuda_math.h:205-210, z_yooji_cuda_volume_integrator.cu:344-347),
+// bit for bit, at the price of a reciprocal instead of two divisions for all
+// but a few voxels.
+//
+// u' = RN(RN(K0 x * rcp(z)) + K2) differs from u = RN(RN(K0 x / z) + K2) by
+// at most 2^-22 |K0 x / z| + ulp(u): rcp has at most 1 ulp of error and each
+// product / sum one rounding.  A pixel inside an image of at most 2048
+// columns needs |u| < 2048, so |K0 x / z| < 2048 + |K2| < 6144 when
+// |K2| < 4096, and |u' - u| < 1.5e-3 + 2.5e-4 < 2^-8 =: m.  If u' is farther
+// than m from every half-integer, no rounding boundary lies between u and
+// u', so rint(u') = rint(u).  Otherwise, and for z <= 1e-4 (or NaN), the
+// IEEE divisions run.  (Outside the image both forms give columns out of
+// range, where the exact value does not matter.)  `fast` is false when the
+// principal point is out of the bound.
+__device__ __forceinline__ void nearest_pixel(float x, float y, float z, const float* K, bool fast, int& px,
+                                              int& py) {
+  constexpr float kEdge = 0.5f - 1.0f / 256.0f;
+  const float a = K[0] * x, b = K[1] * y;
+  float u = 0.0f, v = 0.0f;
+  bool exact = !(fast && z > 1e-4f);
+  if (!exact) {
+    const float r = rcp_approx(z);
+    u = a * r + K[2];
+    v = b * r + K[3];
+    exact = fabsf(u - rintf(u)) > kEdge || fabsf(v - rintf(v)) > kEdge;
+  }
+  if (exact) {
+    u = a / z + K[2];
+    v = b / z + K[3];
+  }
+  px = __float2int_rn(u);
+  py = __float2int_rn(v);
+}
+
+// g_ctvc's depth update, per voxel in the reference's operation order
+// (z_yooji_cuda_volume_integrator.cu:340-402): world centre p_g, camera point
+// T_gc p_g, nearest pixel, depth d; lambda^-1 |p_g - C|; sdf = d - that;
+// skip if sdf < -mu; tsdf = min(1, sdf / mu); weighted mean with the old
+// value; weight + 1.  The weights and the skip decisions are bit-identical
+// to that order.  Two rewrites that keep every rounding:
+//  * a lane's voxels share their y coordinate, take kPerVec x and kLaneVec
+//    z values, so the partial sums M0 x + M1 y (and M4, M8 rows) and
+//    (x - Cx)^2 + (y - Cy)^2 are formed once per x value, and the rest of
+//    each sum is added in the same order as the full expression;
+//  * the pixel rounding uses nearest_pixel above.
+// The one change of a rounding: sdf / mu is the product with 1 / mu and one
+// Markstein correction step (q = s r; e = fma(-q, mu, s); q + e r, P.
+// Markstein, IBM J. Res. Dev. 34(1), 1990), which returns the IEEE quotient in
+// all but rare cases and otherwise differs by one ulp (6e-8 of a TSDF value,
+// below 0.002 of an int16 step), inside the one-step tolerance.
 template <class S, bool COLOR>
-__global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
+__global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
     k_integrate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
                 const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext, int color) {
   __shared__ uint32_t pre[kMaxSlots + 1];  // prefix of the slots' active-brick counts
+  // per thread, per x value of its voxels: the transform rows' partial sums
+  // M0 x + M1 y, M4 x + M5 y, M8 x + M9 y and (x - Cx)^2 + (y - Cy)^2
+  // ([x value][thread]: a warp's 16-byte reads are consecutive, no bank conflicts)
+  __shared__ float4 xpart[16 / sizeof(typename S::word)][kIntThreads];
   const int n = bt->n;
   if (threadIdx.x < 32) {
     const int ln = threadIdx.x;
@@ -302,15 +411,26 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
   const uint32_t total = pre[n];
 
   typedef typename S::word word;
-  constexpr int kPerVec = 16 / sizeof(word);
-  constexpr int kVecs = kBrickVox / kPerVec;  // 16-byte vectors per brick
-  constexpr int kLaneVec = kVecs / 32;        // vectors per lane
-  constexpr int kLaneVox = kLaneVec * kPerVec;  // 16 voxels per lane
-  constexpr int kRound = 8;
+  constexpr int kPerVec = 16 / sizeof(word);    // voxels per 16-byte vector, consecutive in x
+  constexpr int kVecs = kBrickVox / kPerVec;    // 16-byte vectors per brick
+  constexpr int kLaneVec = kVecs / 32;          // vectors per lane, one z value each
+  constexpr int kRV = 4 / kPerVec > 0 ? 4 / kPerVec : 1;  // 16-byte vectors per round
+  constexpr int kRound = kRV * kPerVec;                    // 4 voxels per round, gathers in flight together
+  constexpr int kRounds = kLaneVec / kRV;
   const int lane = threadIdx.x & 31;
   const int gwarp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  // the lane's voxel coordinates inside a brick: word (k * 32 + lane) * kPerVec + e
+  // is x = x0 + e, y = y0, z = z0 + k * kPerVec / 2
+  const int x0 = (lane * kPerVec) & 7, y0 = ((lane * kPerVec) >> 3) & 7, z0 = (lane * kPerVec) >> 6;
+  constexpr int kZStep = kPerVec / 2;
+  // Per-session values: the voxel loop's in registers (VoxParams); the
+  // brick-level ones (pointers, rotation, centre, brick grid) are read from
+  // the session record at each brick, so they hold no registers across the
+  // loop.  The colour variant keeps the whole IntParams for color_round.
   IntParams q;
+  VoxParams vp;
+  const SessionDev* __restrict__ sp = nullptr;
   int cur = -1;
 
   for (uint32_t i = gwarp; i < total; i += nwarps) {
@@ -324,111 +444,158 @@ __global__ void __launch_bounds__(kIntThreads, VS_INT_MIN_BLOCKS)
     }
     if (lo != cur) {
       cur = lo;
-      load_params(q, bt->s[lo], depth_ext, Tgc_ext, Tcg_ext);
-      if (!color) q.col = nullptr;
+      sp = bt->s[lo];
+      load_vox_params(vp, sp, depth_ext);
+      if (COLOR) {
+        load_params(q, sp, depth_ext, Tgc_ext, Tcg_ext);
+        if (!color) q.col = nullptr;
+      }
     }
-    const uint32_t b = q.list[i - pre[lo]];
+    const uint32_t b = reload(sp->brick_list + (i - pre[lo]));
     int nupd = 0;
-    const int bx = (int)(b % (uint32_t)q.nb0), by = (int)((b / (uint32_t)q.nb0) % (uint32_t)q.nb1),
-              bz = (int)(b / ((uint32_t)q.nb0 * (uint32_t)q.nb1));
-    uint4* bv = reinterpret_cast<uint4*>(reinterpret_cast<word*>(q.vol) + (size_t)b * kBrickVox);
-    const float* __restrict__ lx = q.lut_vox;
-    const float* __restrict__ ly = q.lut_vox + q.d0;
-    const float* __restrict__ lz = q.lut_vox + q.d0 + q.d1;
-    const float* __restrict__ rx_t = q.lut_ray;
-    const float* __restrict__ ry_t = q.lut_ray + q.W;
-    // the lane's 16 voxels: all vector reads first, then two rounds of eight
-    // voxels whose depth (and ray-scale) gathers are in flight together
-    uint4 raw[kLaneVec];
+    const uint32_t nb0 = (uint32_t)reload(&sp->nb[0]), nb1 = (uint32_t)reload(&sp->nb[1]);
+    const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / (nb0 * nb1));
+    uint4* bv = reinterpret_cast<uint4*>(reinterpret_cast<word*>(reload(&sp->vol)) + (size_t)b * kBrickVox);
+    const int d0 = reload(&sp->dim[0]), d1 = reload(&sp->dim[1]);
+    const float* __restrict__ lx = reload(&sp->lut_vox);
+    const float* __restrict__ ly = lx + d0;
+    const float* __restrict__ lz = lx + d0 + d1;
+    // per-x partial sums of the transform rows and of |p_g - C|^2
+    const float* Tg = Tgc_ext ? Tgc_ext : reload(&sp->pose)->Tgc;
+    const float* Tc = Tcg_ext ? Tcg_ext : reload(&sp->pose)->Tcg;
+    float Tr[12];
 #pragma unroll
-    for (int k = 0; k < kLaneVec; k++) raw[k] = bv[k * 32 + lane];
-    word wv[kLaneVec][kPerVec];
+    for (int k = 0; k < 12; k++) Tr[k] = reload(Tg + k);
+    const float C0 = reload(Tc + 3), C1 = reload(Tc + 7), C2 = reload(Tc + 11);
+    const float py = __ldg(ly + by * 8 + y0);
+    const float dy = py - C1;
+    // kept in shared memory (one 16-byte read per voxel) rather than in 16
+    // registers per thread
 #pragma unroll
-    for (int k = 0; k < kLaneVec; k++) memcpy(wv[k], &raw[k], 16);
-    bool changed[kLaneVec];
+    for (int e = 0; e < kPerVec; e++) {
+      const float px = __ldg(lx + bx * 8 + x0 + e);
+      const float dx = px - C0;
+      xpart[e][threadIdx.x] = make_float4(Tr[0] * px + Tr[1] * py, Tr[4] * px + Tr[5] * py, Tr[8] * px + Tr[9] * py,
+                          dx * dx + dy * dy);
+    }
+    // Rounds of kRV vectors (4 voxels): the next round's vectors are read
+    // while this round's voxels run, and a round's vectors are written back
+    // as soon as it ends, so at most two rounds of voxel words are live.
+    uint4 cur[kRV], nxt[kRV];
 #pragma unroll
-    for (int k = 0; k < kLaneVec; k++) changed[k] = false;
+    for (int v = 0; v < kRV; v++) cur[v] = bv[v * 32 + lane];
 #pragma unroll
-    for (int r = 0; r < kLaneVox / kRound; r++) {
+    for (int r = 0; r < kRounds; r++) {
+      if (r + 1 < kRounds) {
+#pragma unroll
+        for (int v = 0; v < kRV; v++) nxt[v] = bv[((r + 1) * kRV + v) * 32 + lane];
+      }
+      word wv[kRV][kPerVec];
+#pragma unroll
+      for (int v = 0; v < kRV; v++) memcpy(wv[v], &cur[v], 16);
+      // this round's z values, one per vector
+      float tz0[kRV], tz1[kRV], tz2[kRV], dz2[kRV];
+#pragma unroll
+      for (int v = 0; v < kRV; v++) {
+        const float pz = __ldg(lz + bz * 8 + z0 + (r * kRV + v) * kZStep);
+        tz0[v] = Tr[2] * pz;
+        tz1[v] = Tr[6] * pz;
+        tz2[v] = Tr[10] * pz;
+        const float dz = pz - C2;
+        dz2[v] = dz * dz;
+      }
+      // nearest pixel of every voxel, then its gathers, all in flight together
+      float2 g[kRound];
       int pix[kRound];
-      float dm[kRound], lam[kRound];
+#pragma unroll
+      for (int j = 0; j < kRound; j++) {
+        const int v = j / kPerVec, e = j % kPerVec;
+        float told;
+        uint32_t wold;
+        S::decode(wv[v][e], told, wold);
+        pix[j] = -1;
+        if ((float)wold >= vp.max_w) continue;
+        // T_gc p_g, each row summed as M0 x + M1 y + M2 z + M3
+        const float4 xp = xpart[e][threadIdx.x];
+        const float cx = (xp.x + tz0[v]) + Tr[3];
+        const float cy = (xp.y + tz1[v]) + Tr[7];
+        const float cz = (xp.z + tz2[v]) + Tr[11];
+        int x, y;
+        nearest_pixel(cx, cy, cz, vp.K, vp.fast, x, y);
+        if ((unsigned)x > (unsigned)(vp.W - 1) || (unsigned)y > (unsigned)(vp.H - 1)) continue;
+        pix[j] = y * vp.W + x;
+      }
+#pragma unroll
+      for (int j = 0; j < kRound; j++) {
+        g[j] = make_float2(0.0f, 0.0f);
+        if (pix[j] >= 0) {
+          if (vp.packed) {
+            g[j] = __ldg(reinterpret_cast<const float2*>(vp.src) + pix[j]);
+          } else {
+            g[j].x = __ldg(reinterpret_cast<const float*>(vp.src) + pix[j]);
+            if (vp.lam) g[j].y = __ldg(vp.lam + pix[j]);
+          }
+        }
+      }
+      bool changed[kRV];
+#pragma unroll
+      for (int v = 0; v < kRV; v++) changed[v] = false;
       unsigned upd = 0u;  // voxels of this round whose depth was updated
 #pragma unroll
       for (int j = 0; j < kRound; j++) {
-        const int v = r * kRound + j, k = v / kPerVec, e = v % kPerVec;
-        const int li = (k * 32 + lane) * kPerVec + e;
-        const int xc = bx * 8 + (li & 7), yc = by * 8 + ((li >> 3) & 7), zc = bz * 8 + (li >> 6);
+        const int v = j / kPerVec, e = j % kPerVec;
+        if (pix[j] < 0 || !(g[j].x > 0.0f)) continue;
         float told;
         uint32_t wold;
-        S::decode(wv[k][e], told, wold);
-        pix[j] = -1;
-        if ((float)wold >= q.max_w) continue;
-        const F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
-        const F3 pc = transform(pg, q.T);
-        float u, vv;
-        project(pc, q.K, u, vv);
-        const int x = __float2int_rn(u), y = __float2int_rn(vv);
-        if (x < 0 || x > q.W - 1 || y < 0 || y > q.H - 1) continue;
-        pix[j] = y * q.W + x;
-      }
-#pragma unroll
-      for (int j = 0; j < kRound; j++) {
-        dm[j] = 0.0f;
-        lam[j] = 0.0f;
-        if (pix[j] >= 0) {
-          dm[j] = __ldg(q.depth + pix[j]);
-          if (q.lam_map) lam[j] = __ldg(q.lam_map + pix[j]);
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < kRound; j++) {
-        const int v = r * kRound + j, k = v / kPerVec, e = v % kPerVec;
-        if (pix[j] < 0 || !(dm[j] > 0.0f)) continue;
-        const int li = (k * 32 + lane) * kPerVec + e;
-        const int xc = bx * 8 + (li & 7), yc = by * 8 + ((li >> 3) & 7), zc = bz * 8 + (li >> 6);
-        float told;
-        uint32_t wold;
-        S::decode(wv[k][e], told, wold);
+        S::decode(wv[v][e], told, wold);
         const float oldW = (float)wold;
-        float lm = lam[j];
-        if (!q.lam_map) {
-          const int x = pix[j] % q.W, y = pix[j] / q.W;
-          const float rx = __ldg(rx_t + x), ry = __ldg(ry_t + y);
+        float lm = g[j].y;
+        if (!vp.packed && !vp.lam) {
+          const float* rx_t = reload(&sp->lut_ray);
+          const int x = pix[j] % vp.W, y = pix[j] / vp.W;
+          const float rx = __ldg(rx_t + x), ry = __ldg(rx_t + vp.W + y);
           lm = 1.0f / sqrtf(rx * rx + ry * ry + 1.0f);
         }
-        const F3 pg = f3(__ldg(lx + xc), __ldg(ly + yc), __ldg(lz + zc));
-        const F3 dc = f3(pg.x - q.C[0], pg.y - q.C[1], pg.z - q.C[2]);
-        const float nrm = sqrtf(dc.x * dc.x + dc.y * dc.y + dc.z * dc.z);
-        const float sdf = dm[j] - lm * nrm;
-        if (sdf < -q.mu) continue;
-        const float ts = fminf(1.0f, sdf / q.mu);
+        const float nrm = sqrtf(xpart[e][threadIdx.x].w + dz2[v]);
+        const float sdf = g[j].x - lm * nrm;
+        if (sdf < -vp.mu) continue;
+        const float q0 = sdf * vp.inv_mu;
+        const float ts = fminf(1.0f, fmaf(fmaf(-q0, vp.mu, sdf), vp.inv_mu, q0));
         const float newW = oldW + 1.0f;
         const float inewW = __ldg(g_inv_weight + (int)newW);
         const float tnew = (oldW * told + ts) * inewW;
-        wv[k][e] = S::encode(tnew, (uint32_t)newW);
-        changed[k] = true;
+        wv[v][e] = S::encode(tnew, (uint32_t)newW);
+        changed[v] = true;
         upd |= 1u << j;
         nupd++;
       }
-      if (COLOR && q.col && upd) color_round<S, kPerVec>(q, upd, r * kRound, lane, bx, by, bz, b, wv, lx, ly, lz);
-    }
+      if (COLOR && q.col && upd)
+        color_round<S, kPerVec, kRound>(q, upd, r * kRound, lane, bx, by, bz, b, wv, lx, ly, lz);
 #pragma unroll
-    for (int k = 0; k < kLaneVec; k++)
-      if (changed[k]) {
-        memcpy(&raw[k], wv[k], 16);
-        bv[k * 32 + lane] = raw[k];
+      for (int v = 0; v < kRV; v++)
+        if (changed[v]) {
+          memcpy(&cur[v], wv[v], 16);
+          bv[(r * kRV + v) * 32 + lane] = cur[v];
+        }
+      if (r + 1 < kRounds) {
+#pragma unroll
+        for (int v = 0; v < kRV; v++) cur[v] = nxt[v];
       }
+    }
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
     if (lane == 0) {
       if (nupd) {
-        atomicAdd(q.counters + 1, (uint32_t)nupd);
+        atomicAdd(reload(&sp->brick_count) + 1, (uint32_t)nupd);
         // weights never decrease, so a brick that got an update, and the
         // occupancy cells around it, stay occupied
-        if (q.occ) {
-          set_bit_once(q.occ, b);
-          set_bit_once(q.occ1, occ_cell(bx, by, bz, kOcc1Shift, q.nc1));
-          set_bit_once(q.occ2, occ_cell(bx, by, bz, kOcc2Shift, q.nc2));
+        uint32_t* occ = reload(&sp->occ);
+        if (occ) {
+          const int nc1[2] = {reload(&sp->nc1[0]), reload(&sp->nc1[1])};
+          const int nc2[2] = {reload(&sp->nc2[0]), reload(&sp->nc2[1])};
+          set_bit_once(occ, b);
+          set_bit_once(reload(&sp->occ1), occ_cell(bx, by, bz, kOcc1Shift, nc1));
+          set_bit_once(reload(&sp->occ2), occ_cell(bx, by, bz, kOcc2Shift, nc2));
         }
       }
     }

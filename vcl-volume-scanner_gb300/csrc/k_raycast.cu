@@ -315,8 +315,13 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
     }
     if (tsdf == 1.0f && state != BEHIND && --recheck < 0) {
       // While samples read "no value" (TSDF 1) the state and the step stay as
-      // they are, so the steps of a free-space run are replayed with the same
-      // float operations as the loop above, without the volume reads.
+      // they are, so the `run` steps of a free-space run are taken at once:
+      // p + run * inc and total + run * sn.  The step-by-step sums of the
+      // reference round after every step; the jump rounds once, so the
+      // position after a run differs from theirs by at most a few ulps of the
+      // voxel coordinate (under 1e-3 voxel for coordinates below 1024), which
+      // moves the later samples and the surface point by far less than the
+      // 1 mm ray-cast tolerance.
       const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
       const F3 inc = scale(sn, rd);
       int m = V.free_run(vs, inc);
@@ -330,10 +335,10 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
       // ray then ends without a hit whichever step it was.
       const bool capped = m > cap - it;
       const int run = capped ? cap - it : m;
-#pragma unroll 4
-      for (int k = 0; k < run; k++) {
-        vs = add(vs, inc);
-        total += sn;
+      if (run > 0) {
+        const float fr = (float)run;
+        vs = add(vs, scale(fr, inc));
+        total += fr * sn;
       }
       if (total > total_max) return false;
       it += run;

@@ -288,7 +288,7 @@ size_t vs_session_bytes(const vs_config* c) {
   b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + sizeof(BatchTable) + 64;
   b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
   for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
-  b += (size_t)w * h * 4;                                                      // ray-scale map
+  b += (size_t)w * h * (4 + 8);                                                // ray-scale map, {depth, scale} map
   if (c->color) {
     b += (size_t)c->dim[0] * c->dim[1] * c->dim[2] * 4 + (size_t)w * h * (3 + 4);  // colour volume and frame
     for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 4;      // colour maps
@@ -355,6 +355,7 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.lut_vox, (size_t)(h.dim[0] + h.dim[1] + h.dim[2]) * 4);
   rc |= alloc(s, &h.lut_ray, (size_t)(h.lv[0].W + h.lv[0].H) * 4);
   rc |= alloc(s, &h.lam_map, n0 * 4);
+  rc |= alloc(s, &h.dl_map, n0 * 8);
   if (cfg->color) {
     rc |= alloc(s, &h.col, nbr * kBrickVox * 4);
     rc |= alloc(s, &h.rgb_in, n0 * 3);

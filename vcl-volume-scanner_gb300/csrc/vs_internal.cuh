@@ -99,6 +99,8 @@ struct SessionDev {
   uint32_t* rgb_packed;          // the same frame as one 0x00BBGGRR word per pixel
   uint32_t* m_rgb[kMaxLevels];   // ray-cast colour per pixel, 0x00BBGGRR
   float* lam_map;                // level-0 ray scale per pixel (NULL: computed per voxel)
+  float2* dl_map;                // level-0 {depth (m), ray scale} per pixel, written by the ingest: one
+                                 // gather per voxel in the integration (NULL: depth_raw and lam_map)
 };
 
 // Sessions advanced together by one launch of every per-frame kernel.  The
