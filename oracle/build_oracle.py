@@ -1,6 +1,9 @@
 """Build recipe for the oracle (test infrastructure only).
 
-* oracle/_build/liboracle.so  -- the C++ restatement (oracle.cpp), always.
+* oracle/_build/liboracle.so  -- the C++ restatement (oracle.cpp), always,
+  with the seeded synthetic-input generator (the package's csrc/synth.cpp)
+  compiled in, so that a CPU run of the oracle maps no library of the
+  package.
 * oracle/_ref/libref_pin.so   -- the reference's own _yooji_math_inlines.h
   compiled from the reference tree, only where that tree is present.
 * oracle/_ref/libref_pin_cuda.so -- the reference's own _yooji_cuda_math.h
@@ -22,7 +25,10 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF_UTIL = "/root/reference/VCL_Volume_Scanner/STAC/Util"
+# the reference tree: VS_REFERENCE_ROOT, by default where it is mounted here
+REF_ROOT = os.environ.get("VS_REFERENCE_ROOT", "/root/reference")
+REF_UTIL = os.path.join(REF_ROOT, "VCL_Volume_Scanner", "STAC", "Util")
+SYNTH_DIR = os.path.join(os.path.dirname(HERE), "vcl-volume-scanner_gb300", "csrc")
 CXX = os.environ.get("CXX", "g++")
 FLAGS = ["-O2", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared"]
 
@@ -38,10 +44,12 @@ def build_oracle(force=False):
     """OpenMP parallelises the per-pixel / per-sub-cube loops only; every
     result is independent of the thread count (OMP_NUM_THREADS)."""
     out = os.path.join(HERE, "_build", "liboracle.so")
-    srcs = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle.h")]
+    synth = os.path.join(SYNTH_DIR, "synth.cpp")
+    srcs = [os.path.join(HERE, "oracle.cpp"), os.path.join(HERE, "oracle.h"), synth,
+            os.path.join(SYNTH_DIR, "vs_synth.h")]
     if force or not _newer(out, srcs):
         os.makedirs(os.path.dirname(out), exist_ok=True)
-        subprocess.check_call([CXX] + FLAGS + ["-fopenmp", "-o", out, srcs[0]])
+        subprocess.check_call([CXX] + FLAGS + ["-fopenmp", "-pthread", "-I", SYNTH_DIR, "-o", out, srcs[0], synth])
     return out
 
 

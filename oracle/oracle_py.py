@@ -53,6 +53,10 @@ def load():
         path = _b.build_oracle()
         lib = ctypes.CDLL(path)
         P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        lib.vs_synth_default.restype = None
+        lib.vs_synth_default.argtypes = [ctypes.POINTER(SynthConfig), I, I]
+        lib.vs_synth_generate.restype = I
+        lib.vs_synth_generate.argtypes = [ctypes.POINTER(SynthConfig), P, P, P]
         sig = {
             "or_depth_to_m": (None, [P, I, F, P]),
             "or_gaussian_table": (None, [F, I, P]),
@@ -140,6 +144,10 @@ def load_ref_pin_cuda():
             return None
         lib = ctypes.CDLL(path)
         P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
+        lib.vs_synth_default.restype = None
+        lib.vs_synth_default.argtypes = [ctypes.POINTER(SynthConfig), I, I]
+        lib.vs_synth_generate.restype = I
+        lib.vs_synth_generate.argtypes = [ctypes.POINTER(SynthConfig), P, P, P]
         sig = {
             "ref_lld6": (I, [P, P]), "ref_sls6": (I, [P, P, P]),
             "ref_giv": (I, [F, F, I, I, P, P]), "ref_gin": (I, [F, F, I, I, P, P]),
@@ -269,6 +277,50 @@ def warp_depth(depth_m, Kd, T_rgb_wrt_d, Kr, wr, hr):
     load().or_warp_depth(_p(d), wd, hd, _p(np.asarray(Kd, np.float32)), _p(np.asarray(T_rgb_wrt_d, np.float32).ravel()),
                          _p(np.asarray(Kr, np.float32)), wr, hr, _p(out))
     return out
+
+
+class SynthConfig(ctypes.Structure):
+    """vs_synth_config (the synthetic-input generator compiled into the
+    oracle library, the same source as the package's)"""
+    _fields_ = [
+        ("width", ctypes.c_int), ("height", ctypes.c_int),
+        ("fx", ctypes.c_float), ("fy", ctypes.c_float), ("cx", ctypes.c_float), ("cy", ctypes.c_float),
+        ("n_frames", ctypes.c_int),
+        ("seed", ctypes.c_uint64),
+        ("orbit_radius", ctypes.c_double),
+        ("view_distance", ctypes.c_double),
+        ("orbit_start_deg", ctypes.c_double),
+        ("orbit_step_deg", ctypes.c_double),
+        ("jitter_deg", ctypes.c_double),
+        ("jitter_m", ctypes.c_double),
+        ("noise", ctypes.c_int),
+        ("dropout_iid", ctypes.c_double),
+        ("dropout_blob", ctypes.c_double),
+        ("max_depth", ctypes.c_double),
+        ("threads", ctypes.c_int),
+    ]
+
+
+def synth_config(width, height, **kw):
+    lib = load()
+    c = SynthConfig()
+    lib.vs_synth_default(ctypes.byref(c), width, height)
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def synth_generate(cfg):
+    """(depth uint16 [n,h,w], T_gc float64 [n,4,4], scene centre) from the
+    oracle library's copy of the generator (bit-identical to the package's)"""
+    lib = load()
+    n, h, w = cfg.n_frames, cfg.height, cfg.width
+    depth = np.empty((n, h, w), np.uint16)
+    T = np.empty((n, 4, 4), np.float64)
+    c = np.empty(3, np.float64)
+    if lib.vs_synth_generate(ctypes.byref(cfg), _p(depth), _p(T), _p(c)) != 0:
+        raise ValueError("bad synth config")
+    return depth, T, c
 
 
 def depth_to_m(mm, scale=0.001):
