@@ -144,10 +144,6 @@ def load_ref_pin_cuda():
             return None
         lib = ctypes.CDLL(path)
         P, I, F = ctypes.c_void_p, ctypes.c_int, ctypes.c_float
-        lib.vs_synth_default.restype = None
-        lib.vs_synth_default.argtypes = [ctypes.POINTER(SynthConfig), I, I]
-        lib.vs_synth_generate.restype = I
-        lib.vs_synth_generate.argtypes = [ctypes.POINTER(SynthConfig), P, P, P]
         sig = {
             "ref_lld6": (I, [P, P]), "ref_sls6": (I, [P, P, P]),
             "ref_giv": (I, [F, F, I, I, P, P]), "ref_gin": (I, [F, F, I, I, P, P]),
