@@ -346,7 +346,9 @@ int vs_get_device_buffer(vs_session* s, int which, void** ptr);
  *   volume_dev: (dim/8)^3 sub-cubes of 512 uint32 words each, sub-cubes x
  *     fastest then y then z, voxels x fastest inside a sub-cube; a word is
  *     (uint16 weight << 16) | uint16(int16 q) with TSDF = q / 32767.  A new
- *     volume is every word 0x00007FFF (TSDF 1, weight 0).
+ *     volume is every word 0x00007FFF (TSDF 1, weight 0).  It must be
+ *     16-byte aligned (sub-cubes move as 16-byte vectors); another address
+ *     returns VS_ERR_ARG before anything runs.
  *   dim, origin: 3 ints / 3 floats; K: host fx, fy, cx, cy; depth ww x hh
  *   float metres and the 4x4 poses on the device, as vs_integrate_depth. */
 int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, const float* origin,

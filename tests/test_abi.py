@@ -5,6 +5,7 @@ import ctypes
 import os
 import re
 
+import numpy as np
 import pytest
 
 import vs_scanner as V
@@ -80,3 +81,21 @@ def test_no_gpu_means_error_not_fallback(built):
     h = ctypes.c_void_p()
     rc = V.load().vs_session_create(ctypes.byref(_cfg()), ctypes.byref(h))
     assert rc == V.VS_ERR_CUDA
+
+
+def test_noalloc_rejects_a_misaligned_volume_before_any_launch(built):
+    """the allocation-free entry point checks the caller's volume pointer
+    (16-byte aligned) before it touches the GPU, so the call fails the same
+    way with or without a device"""
+    import vs_scanner as V
+
+    lib = V.load()
+    dim = np.array([64, 64, 64], np.int32)
+    origin = np.zeros(3, np.float32)
+    K = np.array([525.0, 525.0, 319.5, 239.5], np.float32)
+    p = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    fake = ctypes.c_void_p(0x10008)  # 8-byte aligned only; never dereferenced
+    rc = lib.vs_integrate_depth_noalloc(fake, p(dim), p(origin), 0.005, 0.02, 100.0, fake, 640, 480, p(K), fake,
+                                        fake, None)
+    assert rc == V.VS_ERR_ARG
+    assert b"16-byte aligned" in lib.vs_last_error()

@@ -40,8 +40,9 @@ def _host_args(cfg):
     return dim, origin, K
 
 
-def test_noalloc_matches_session_entry_point_on_two_calls(gpu):
-    case = helpers.make_case(width=160, height=120, dim=128, frames=2, seed=3)
+def _compare_two_calls(case):
+    """two integrations, each through the session entry point and through the
+    allocation-free one, compared after each call"""
     cfg = case["cfg"]
     lib = V.load()
     dim, origin, K = _host_args(cfg)
@@ -69,6 +70,27 @@ def test_noalloc_matches_session_entry_point_on_two_calls(gpu):
             m = w_ref > 0
             assert m.sum() > 10000
             assert np.max(np.abs(q[m] - helpers.q16(t_ref[m]))) <= 1, k
+
+
+def test_noalloc_matches_session_entry_point_on_two_calls(gpu):
+    _compare_two_calls(helpers.make_case(width=160, height=120, dim=128, frames=2, seed=3))
+
+
+def test_noalloc_non_cubic_volume_maps_sub_cubes_like_the_session(gpu):
+    case = helpers.make_case(width=160, height=120, dim=128, frames=2, seed=3)
+    cfg = case["cfg"]
+    # 64 x 128 x 96 voxels around the same scene: sub-cube indices differ per axis
+    cfg.dim[0], cfg.dim[1], cfg.dim[2] = 64, 128, 96
+    for k in range(3):
+        cfg.origin[k] = float(case["centre"][k]) - 0.5 * cfg.dim[k] * cfg.voxel_size
+    _compare_two_calls(case)
+
+
+def test_noalloc_accepts_a_volume_at_its_cap(gpu):
+    """512^3 voxels (262,144 sub-cubes, the scratch's maximum) is accepted and
+    integrates like the session entry point"""
+    case = helpers.make_case(width=160, height=120, dim=512, size=1.0, frames=2, seed=3)
+    _compare_two_calls(case)
 
 
 def test_noalloc_rejects_volumes_beyond_its_scratch(gpu):

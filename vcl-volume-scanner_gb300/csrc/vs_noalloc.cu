@@ -27,10 +27,16 @@
 // GPU (different streams, or different host threads) race on the scratch.
 //
 // The kernels are the session path's own activation and update kernels
-// (k_integrate.cu), handed a descriptor that lives in the scratch array.
+// (k_integrate.cu), handed a descriptor that lives in the scratch array.  The
+// descriptor and the work table reach the scratch as kernel arguments (one
+// set-up kernel copies them and clears the flags), so no host buffer is read
+// after the call returns.  The set-up of the per-call tables also rewrites
+// the library's shared table of 1/w (w = 1..65535) with the same values
+// every call; session integrations running meanwhile read identical numbers.
 #include <cuda_runtime.h>
 
 #include <cstddef>
+#include <cstdint>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -59,6 +65,20 @@ static_assert(sizeof(SessionDev) <= kDescBytes, "descriptor does not fit its scr
 static_assert(sizeof(BatchTable) <= kTableBytes, "work table does not fit its scratch slot");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+static_assert(sizeof(SessionDev) + sizeof(BatchTable) + 64 <= 32764, "set-up arguments exceed the parameter space");
+
+// copies the call's descriptor and work table into the scratch and clears
+// the activation flags of the volume's sub-cubes
+__global__ void k_noalloc_setup(const SessionDev h, const BatchTable t, SessionDev* d, BatchTable* dt,
+                                uint32_t* flags, uint32_t nbr) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr uint32_t kHw = sizeof(SessionDev) / 4, kTw = sizeof(BatchTable) / 4;
+  static_assert(sizeof(SessionDev) % 4 == 0 && sizeof(BatchTable) % 4 == 0, "word copies");
+  if (i < kHw) reinterpret_cast<uint32_t*>(d)[i] = reinterpret_cast<const uint32_t*>(&h)[i];
+  if (i < kTw) reinterpret_cast<uint32_t*>(dt)[i] = reinterpret_cast<const uint32_t*>(&t)[i];
+  for (uint32_t k = i; k < nbr; k += gridDim.x * blockDim.x) flags[k] = 0u;
+}
 
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
@@ -95,6 +115,8 @@ extern "C" int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, 
                                           const float* T_cg_dev, void* stream) {
   if (!volume_dev || !dim || !origin || !map_depth_dev || !K || !T_gc_dev || !T_cg_dev)
     return fail(VS_ERR_ARG, "null argument");
+  if (reinterpret_cast<uintptr_t>(volume_dev) % 16)
+    return fail(VS_ERR_ARG, "volume_dev must be 16-byte aligned (sub-cubes are read and written as 16-byte vectors)");
   for (int k = 0; k < 3; k++)
     if (dim[k] < 8 || dim[k] % 8 || dim[k] > integrate_max_dim())
       return fail(VS_ERR_ARG, "volume dims must be multiples of 8 in 8..1024");
@@ -139,9 +161,8 @@ extern "C" int vs_integrate_depth_noalloc(uint32_t* volume_dev, const int* dim, 
   const SessionDev* hr = &h;
   const SessionDev* dr = d;
   fill_batch_table(t, &hr, &dr, 1);
-  cudaError_t e = cudaMemcpyAsync(d, &h, sizeof(SessionDev), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(dt, &t, sizeof(BatchTable), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(h.brick_flag, 0, nbr * sizeof(uint32_t), st);
+  k_noalloc_setup<<<512, 256, 0, st>>>(h, t, d, dt, h.brick_flag, (uint32_t)nbr);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return fail(VS_ERR_CUDA, std::string("scratch set-up: ") + cudaGetErrorString(e));
   launch_session_tables(h, d, st);
   // counters are cleared inside launch_integrate

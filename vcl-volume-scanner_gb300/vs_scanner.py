@@ -9,7 +9,7 @@ STAC/Engine/CPU/z_yooji_object_scanner.cpp): a ``Session`` carries what
 ``scan_frame``.  Device pointers are passed as integers (for example
 ``torch.Tensor.data_ptr()``); host arrays are numpy arrays.
 
-The library must be built (``build.py``) and a CUDA device present: there is
+The library must be built (``vs_build.py``) and a CUDA device present: there is
 no CPU fallback, and every compute call raises ``VsError`` otherwise.
 """
 import ctypes
