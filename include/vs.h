@@ -260,6 +260,12 @@ int vs_stage_raycast(vs_session* s);
  * [3] frames processed. */
 int vs_get_pose(vs_session* s, float* T_gc, double* T_gc_f64, int* info);
 int vs_set_pose(vs_session* s, const double* T_gc_f64);
+/* the normal equations of the last ICP iteration run (tp_Track_Pose's ATA /
+ * ATb, z_yooji_cuda_pose_tracker.cu:937-943): sums29 = the 21 entries of
+ * the upper triangle of ATA row by row, the 6 of ATb, the correspondence
+ * count and the sum of b^2, as summed (FP64); x6 = the increment solved from
+ * them (twist [w; v], rounded to float).  Either pointer may be NULL. */
+int vs_get_icp_system(vs_session* s, double* sums29, float* x6);
 /* GKvObjectCube::to_host / from_host (_yooji_cuda_object_cube.hpp:6-85): the
  * volume in the reference's x-fastest layout (z*W*H + y*W + x), TSDF as float
  * and weight as uint16; either pointer may be NULL. */

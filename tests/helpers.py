@@ -87,14 +87,18 @@ def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_pose
     filtered input pyramid, input normals, previous pose) to the oracle's
     tracker at every frame: the tracked flag must equal the FP32 oracle's,
     and where both track, the pose must be within 1e-4 rad and 0.1 mm of the
-    FP32 and FP64 oracles' (the per-frame tolerance on identical inputs).
-    Returns the largest rotation (rad) and translation (m) differences and
-    the frames lost."""
+    FP32 and FP64 oracles' (the per-frame tolerance on identical inputs).  A
+    frame whose FP32 and FP64 oracles disagree beyond that tolerance on these
+    inputs is ill-conditioned (the 6x6 system amplifies rounding; a one-pixel
+    change of the coarsest model map can move the solution by a tenth of a
+    radian) and is only counted, not compared.  Returns the largest rotation
+    (rad) and translation (m) differences, the frames lost and a dict with
+    the final pose, volume, maps and the ill-conditioned frames."""
     import torch
 
     ocfg = O.config_from_vs(cfg)
     worst = [0.0, 0.0]
-    lost = []
+    lost, ill = [], []
     with V.Session(cfg) as s:
         for k in range(frames):
             T_prev, T_prev64, _ = s.pose()
@@ -116,7 +120,9 @@ def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_pose
                 if not info[0]:
                     lost.append(k)
                     assert np.array_equal(T64, T_prev64), k  # a lost frame leaves the pose
-                if compare_poses and info[0] and ok64:
+                if compare_poses and info[0] and ok64 and (rot_err(oT, dT) >= 1e-4 or trans_err(oT, dT) >= 1e-4):
+                    ill.append(k)
+                elif compare_poses and info[0] and ok64:
                     for ref in (oT, dT):
                         r, t = rot_err(T64, ref), trans_err(T64, ref)
                         worst[0], worst[1] = max(worst[0], r), max(worst[1], t)
@@ -124,5 +130,6 @@ def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_pose
             s.stage_integrate()
             s.stage_raycast()
             s.sync()
-        final = dict(pose=s.pose()[0], volume=s.volume(), maps=[s.maps(l) for l in range(cfg.levels)])
+        final = dict(pose=s.pose()[0], volume=s.volume(), maps=[s.maps(l) for l in range(cfg.levels)],
+                     ill_conditioned=ill)
     return worst, lost, final

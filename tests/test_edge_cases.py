@@ -15,6 +15,8 @@ import vs_scanner as V
 
 pytestmark = pytest.mark.gpu
 
+torch = pytest.importorskip("torch")
+
 
 def _same_pose(T, oT):
     return helpers.rot_err(T, oT) < 1e-4 and helpers.trans_err(T, oT) < 1e-4
@@ -45,6 +47,16 @@ def test_ragged_image_sizes_match_the_oracle(gpu, size):
     the oracle's ray-cast of the same volume, at every level"""
     w, h = size
     c = helpers.make_case(width=w, height=h, dim=96, size=0.75, frames=3, seed=22)
+    # ingest, filter and pyramid at the ragged size
+    with V.Session(c["cfg"]) as s:
+        d = torch.from_numpy(np.ascontiguousarray(c["depth"][1]).view(np.int16)).cuda()
+        s.stage_filter(d.data_ptr())
+        ref = [O.bilateral(O.depth_to_m(c["depth"][1]))]
+        for l in range(1, 3):
+            ref.append(O.pyramid_down(ref[-1]))
+        for l in range(3):
+            got = s.maps(l)["input_depth"]
+            assert got.shape == ref[l].shape and np.max(np.abs(got - ref[l])) <= 1e-5, l
     _, lost, final = helpers.reanchored_track_check(c["depth"], c["cfg"], 3)
     assert not lost
     vol = O.Volume(c["ocfg"])

@@ -266,79 +266,94 @@ __device__ __forceinline__ void low_rc(int lane, int& r, int& c) {
 
 // The 6x6 solve: d_lld_LL_Decomposition + d_sls_Solve_Linear_System_using_LLD
 // (_yooji_cuda_math.h:489-592), restated as an L D L^T factorisation
-// (D_j = L_jj^2) in float - the reference's own precision, so its pivot rules
-// apply unchanged: a pivot with sqrt(D_j) < 1e-8 fails the solve (returns 1);
+// (D_j = L_jj^2).  The factorisation is done twice.  In float - the
+// reference's own precision - it decides failure by the reference's pivot
+// rules unchanged: a pivot with sqrt(D_j) < 1e-8 fails the solve (returns 1);
 // a negative or NaN pivot makes the reference's square root NaN, its column
 // zero and the solution NaN, which the convergence test reads as converged
-// (returns 2).  The solution is then refined twice against the FP64 normal
-// equations: r = b - A x in double, A d = r with the float factors,
-// x += d in double.  The refined x agrees with an FP64 solve to FP64 rounding
-// for condition numbers up to ~1e6 while the narrow FP64 pipe only carries
-// the residuals.  Lane i < 6 returns x_i.
-__device__ void warp_ldl_solve_f32(float l, float D, int lane, int r, int c, float& v) {
+// (returns 2).  In FP64, from the FP64 sums, it gives the solution: forward
+// and back substitution with the double factors.  Lane i < 6 returns x_i.
+template <class T>
+__device__ void warp_ldl_solve(T l, T D, int lane, T& v) {
   const unsigned M = 0xffffffffu;
   // v: right-hand side in lanes 0..5 on entry, solution on exit
 #pragma unroll
   for (int j = 0; j < 6; j++) {
-    const float vj = __shfl_sync(M, v, j);
+    const T vj = __shfl_sync(M, v, j);
     const bool upd = lane < 6 && lane > j;
-    const float lij = __shfl_sync(M, l, upd ? low_lane(lane, j) : lane);
+    const T lij = __shfl_sync(M, l, upd ? low_lane(lane, j) : lane);
     if (upd) v -= lij * vj;
   }
-  const float dd = __shfl_sync(M, D, lane < 6 ? low_lane(lane, lane) : lane);
+  const T dd = __shfl_sync(M, D, lane < 6 ? low_lane(lane, lane) : lane);
   if (lane < 6) v = v / dd;
 #pragma unroll
   for (int j = 5; j >= 0; j--) {
-    const float xj = __shfl_sync(M, v, j);
+    const T xj = __shfl_sync(M, v, j);
     const bool upd = lane < j;
-    const float lji = __shfl_sync(M, l, upd ? low_lane(j, lane) : lane);
+    const T lji = __shfl_sync(M, l, upd ? low_lane(j, lane) : lane);
     if (upd) v -= lji * xj;
   }
-  (void)r;
-  (void)c;
+}
+
+// in-place L D L^T of the lower triangle held one element per lane (lane
+// low_lane(r, c) holds row r, column c); ok[j] false skips column j's update
+// (the float pass uses it for the reference's failed pivots)
+template <class T>
+__device__ void warp_ldl_factor(T& a, int lane, int r, int c, bool check, bool& fail, bool& nanp) {
+  const unsigned M = 0xffffffffu;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const T d = __shfl_sync(M, a, low_lane(j, j));
+    bool ok = true;
+    if (check) {
+      const bool neg = !(d >= (T)0);
+      const bool tiny = !neg && !(sqrtf((float)d) >= 1e-8f);
+      nanp |= neg;
+      fail |= tiny;
+      ok = !neg && !tiny;
+    } else {
+      ok = d > (T)0;
+      fail |= !ok;
+    }
+    if (lane < 21 && c == j && r > j) a = ok ? a / d : (T)0;
+    const bool upd = lane < 21 && c > j;
+    const T lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
+    const T lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
+    if (upd && ok) a -= lr * d * lc;
+  }
 }
 
 __device__ int warp_solve6(const double* fin, int lane, double& x) {
-  const unsigned M = 0xffffffffu;
   int r = 0, c = 0;
   if (lane < 21) low_rc(lane, r, c);
+  // the reference's decisions, in float
   float a = (lane < 21) ? (float)fin[tri_index(c, r)] : 0.0f;
   bool nanp = false, fail = false;
-#pragma unroll
-  for (int j = 0; j < 6; j++) {
-    const float d = __shfl_sync(M, a, low_lane(j, j));
-    const bool neg = !(d >= 0.0f);
-    const bool tiny = !neg && !(sqrtf(d) >= 1e-8f);
-    nanp |= neg;
-    fail |= tiny;
-    const bool ok = !neg && !tiny;
-    if (lane < 21 && c == j && r > j) a = ok ? a / d : 0.0f;
-    const bool upd = lane < 21 && c > j;
-    const float lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
-    const float lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
-    if (upd && ok) a -= lr * d * lc;
-  }
+  warp_ldl_factor<float>(a, lane, r, c, true, fail, nanp);
   if (fail) return 1;
-  // a now holds L (strict lower part) and D (diagonal lanes)
-  float v = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
-  warp_ldl_solve_f32(a, a, lane, r, c, v);
-  x = (lane < 6) ? (double)v : 0.0;
-  if (nanp) return 2;
-  // iterative refinement on the FP64 system
-  for (int it = 0; it < 2; it++) {
-    double xk[6];
-#pragma unroll
-    for (int k = 0; k < 6; k++) xk[k] = __shfl_sync(M, x, k);
-    double res = 0.0;
-    if (lane < 6) {
-      res = fin[21 + lane];
-#pragma unroll
-      for (int k = 0; k < 6; k++) res -= fin[lane <= k ? tri_index(lane, k) : tri_index(k, lane)] * xk[k];
-    }
-    float dv = (float)res;
-    warp_ldl_solve_f32(a, a, lane, r, c, dv);
-    if (lane < 6) x += (double)dv;
+  if (nanp) {
+    // the reference's solution is NaN here and reads as converged; the pose is
+    // not updated, so the float factors' (finite) solution is only recorded
+    float vf = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
+    warp_ldl_solve<float>(a, a, lane, vf);
+    x = (lane < 6) ? (double)vf : 0.0;
+    return 2;
   }
+  // the solution, in FP64
+  double ad = (lane < 21) ? fin[tri_index(c, r)] : 0.0;
+  bool dfail = false, dnan = false;
+  warp_ldl_factor<double>(ad, lane, r, c, false, dfail, dnan);
+  double v = (lane < 6) ? fin[21 + lane] : 0.0;
+  if (!dfail) {
+    warp_ldl_solve<double>(ad, ad, lane, v);
+  } else {
+    // a pivot that float rounding left positive and FP64 does not (a system
+    // singular to FP64 precision): the float factors' solution
+    float vf = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
+    warp_ldl_solve<float>(a, a, lane, vf);
+    v = (double)vf;
+  }
+  x = (lane < 6) ? v : 0.0;
   return 0;
 }
 

@@ -712,6 +712,15 @@ int vs_get_pose(vs_session* s, float* T_gc, double* T_gc_f64, int* info) {
   return VS_OK;
 }
 
+int vs_get_icp_system(vs_session* s, double* sums29, float* x6) {
+  if (!s) return fail(VS_ERR_ARG, "null session");
+  VS_CU(cudaMemcpyAsync(s->host_pose, s->h.pose, sizeof(Pose), cudaMemcpyDeviceToHost, s->stream));
+  VS_CU(cudaStreamSynchronize(s->stream));
+  if (sums29) std::memcpy(sums29, s->host_pose->last_sums, sizeof(s->host_pose->last_sums));
+  if (x6) std::memcpy(x6, s->host_pose->last_x, sizeof(s->host_pose->last_x));
+  return VS_OK;
+}
+
 int vs_set_pose(vs_session* s, const double* T_gc_f64) {
   if (!s || !T_gc_f64) return fail(VS_ERR_ARG, "null argument");
   double* dT = nullptr;

@@ -138,6 +138,7 @@ _SIGS = {
     "vs_stage_integrate": (_I, [_P]),
     "vs_stage_raycast": (_I, [_P]),
     "vs_get_pose": (_I, [_P, _P, _P, _P]),
+    "vs_get_icp_system": (_I, [_P, _P, _P]),
     "vs_set_pose": (_I, [_P, _P]),
     "vs_get_volume": (_I, [_P, _P, _P]),
     "vs_set_volume": (_I, [_P, _P, _P]),
@@ -466,6 +467,13 @@ class Session:
         info = np.empty(4, np.int32)
         _check(self.lib.vs_get_pose(self.h, _ptr(T), _ptr(Td), _ptr(info)))
         return T.reshape(4, 4), Td.reshape(4, 4), info
+
+    def icp_system(self):
+        """(sums [29] float64, x [6] float32) of the last ICP iteration run"""
+        sums = np.empty(29, np.float64)
+        x = np.empty(6, np.float32)
+        _check(self.lib.vs_get_icp_system(self.h, _ptr(sums), _ptr(x)))
+        return sums, x
 
     def set_pose(self, T_gc):
         Td = np.ascontiguousarray(T_gc, dtype=np.float64).reshape(16)
