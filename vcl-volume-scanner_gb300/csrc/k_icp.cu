@@ -295,63 +295,81 @@ __device__ void warp_ldl_solve(T l, T D, int lane, T& v) {
   }
 }
 
-// in-place L D L^T of the lower triangle held one element per lane (lane
-// low_lane(r, c) holds row r, column c); ok[j] false skips column j's update
-// (the float pass uses it for the reference's failed pivots)
-template <class T>
-__device__ void warp_ldl_factor(T& a, int lane, int r, int c, bool check, bool& fail, bool& nanp) {
-  const unsigned M = 0xffffffffu;
-#pragma unroll
-  for (int j = 0; j < 6; j++) {
-    const T d = __shfl_sync(M, a, low_lane(j, j));
-    bool ok = true;
-    if (check) {
-      const bool neg = !(d >= (T)0);
-      const bool tiny = !neg && !(sqrtf((float)d) >= 1e-8f);
-      nanp |= neg;
-      fail |= tiny;
-      ok = !neg && !tiny;
-    } else {
-      ok = d > (T)0;
-      fail |= !ok;
-    }
-    if (lane < 21 && c == j && r > j) a = ok ? a / d : (T)0;
-    const bool upd = lane < 21 && c > j;
-    const T lr = __shfl_sync(M, a, upd ? low_lane(r, j) : lane);
-    const T lc = __shfl_sync(M, a, upd ? low_lane(c, j) : lane);
-    if (upd && ok) a -= lr * d * lc;
-  }
+// 1 / d in FP64 for a positive pivot d: the float reciprocal refined by two
+// Newton-Raphson steps r <- r + r (1 - d r) (the error squares each step:
+// 2^-23, 2^-46, then below the double rounding), four dependent FP64
+// operations instead of a double division on the narrow FP64 pipe
+__device__ __forceinline__ double recip_f64(double d) {
+  double r = (double)(1.0f / (float)d);
+  if (!(r > 0.0 && r < 1e300)) return 1.0 / d;  // outside the float range
+  double e = fma(-d, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-d, r, 1.0);
+  return fma(r, e, r);
 }
 
+// The two factorisations share one loop over the columns: the float chain
+// (the reference's decisions) and the FP64 chain (the solution) are
+// independent, so the scheduler overlaps their latencies.
 __device__ int warp_solve6(const double* fin, int lane, double& x) {
+  const unsigned M = 0xffffffffu;
   int r = 0, c = 0;
   if (lane < 21) low_rc(lane, r, c);
-  // the reference's decisions, in float
   float a = (lane < 21) ? (float)fin[tri_index(c, r)] : 0.0f;
-  bool nanp = false, fail = false;
-  warp_ldl_factor<float>(a, lane, r, c, true, fail, nanp);
+  double ad = (lane < 21) ? fin[tri_index(c, r)] : 0.0;
+  double inv = 0.0;  // lane j < 6: 1 / D_j of the FP64 factors
+  bool nanp = false, fail = false, dfail = false;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const float d = __shfl_sync(M, a, low_lane(j, j));
+    const double dd = __shfl_sync(M, ad, low_lane(j, j));
+    const bool neg = !(d >= 0.0f);
+    const bool tiny = !neg && !(sqrtf(d) >= 1e-8f);
+    nanp |= neg;
+    fail |= tiny;
+    const bool ok = !neg && !tiny;
+    const bool dok = dd > 0.0;
+    dfail |= !dok;
+    const double di = dok ? recip_f64(dd) : 0.0;
+    if (lane == j) inv = di;
+    if (lane < 21 && c == j && r > j) {
+      a = ok ? a / d : 0.0f;
+      ad = ad * di;
+    }
+    const bool upd = lane < 21 && c > j;
+    const int sr = upd ? low_lane(r, j) : lane, sc = upd ? low_lane(c, j) : lane;
+    const float lr = __shfl_sync(M, a, sr), lc = __shfl_sync(M, a, sc);
+    const double lrd = __shfl_sync(M, ad, sr), lcd = __shfl_sync(M, ad, sc);
+    if (upd && ok) a -= lr * d * lc;
+    if (upd && dok) ad -= lrd * dd * lcd;
+  }
   if (fail) return 1;
-  if (nanp) {
-    // the reference's solution is NaN here and reads as converged; the pose is
-    // not updated, so the float factors' (finite) solution is only recorded
+  if (nanp || dfail) {
+    // nanp: the reference's solution is NaN here and reads as converged; the
+    // pose is not updated, so the float factors' (finite) solution is only
+    // recorded.  dfail: a pivot that float rounding left positive and FP64
+    // does not (a system singular to FP64 precision): the float solution.
     float vf = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
     warp_ldl_solve<float>(a, a, lane, vf);
     x = (lane < 6) ? (double)vf : 0.0;
-    return 2;
+    return nanp ? 2 : 0;
   }
-  // the solution, in FP64
-  double ad = (lane < 21) ? fin[tri_index(c, r)] : 0.0;
-  bool dfail = false, dnan = false;
-  warp_ldl_factor<double>(ad, lane, r, c, false, dfail, dnan);
+  // L D L^T x = b with the FP64 factors and the inverse pivots
   double v = (lane < 6) ? fin[21 + lane] : 0.0;
-  if (!dfail) {
-    warp_ldl_solve<double>(ad, ad, lane, v);
-  } else {
-    // a pivot that float rounding left positive and FP64 does not (a system
-    // singular to FP64 precision): the float factors' solution
-    float vf = (lane < 6) ? (float)fin[21 + lane] : 0.0f;
-    warp_ldl_solve<float>(a, a, lane, vf);
-    v = (double)vf;
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const double vj = __shfl_sync(M, v, j);
+    const bool upd = lane < 6 && lane > j;
+    const double lij = __shfl_sync(M, ad, upd ? low_lane(lane, j) : lane);
+    if (upd) v -= lij * vj;
+  }
+  if (lane < 6) v *= inv;
+#pragma unroll
+  for (int j = 5; j >= 0; j--) {
+    const double xj = __shfl_sync(M, v, j);
+    const bool upd = lane < j;
+    const double lji = __shfl_sync(M, ad, upd ? low_lane(j, lane) : lane);
+    if (upd) v -= lji * xj;
   }
   x = (lane < 6) ? v : 0.0;
   return 0;
@@ -531,6 +549,9 @@ __global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
     // uniform across the session's ranges: no range of this session has
     // closed the iteration yet when any of them reads the flags
     if (iter >= s->iters[level] || (P->skip | P->failed | P->level_done[level])) {
+      // the session sits this launch out (its flags do not change during the
+      // launch): move the counter past its remaining ranges at once
+      if (threadIdx.x == 0) atomicMax(work, (unsigned)pre[slot + 1]);
       __syncthreads();  // every thread has read s_item before the next fetch
       continue;
     }
@@ -610,8 +631,21 @@ __global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
         v.x = 0;
         v.y = 0;
         if (k < 29) {
+          // four partials in flight per thread, combined in the same order
+          // as one at a time (a missing one combines as an exact zero)
           const PT* base = reinterpret_cast<const PT*>(s->partials);
-          for (int bb = j; bb < nvb; bb += 8) v = combine(v, __ldcg(base + (size_t)bb * kPartials + k), MODE);
+          for (int bb = j; bb < nvb; bb += 32) {
+            PT t4[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+              const int q = bb + 8 * u;
+              t4[u].x = 0;
+              t4[u].y = 0;
+              if (q < nvb) t4[u] = __ldcg(base + (size_t)q * kPartials + k);
+            }
+#pragma unroll
+            for (int u = 0; u < 4; u++) v = combine(v, t4[u], MODE);
+          }
         }
 #pragma unroll
         for (int m = 4; m >= 1; m >>= 1) v = combine(v, shfl_xor2(v, m), MODE);
