@@ -421,9 +421,10 @@ int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps,
  * A server takes frames from many sessions as they arrive and runs them with
  * continuous batching: a worker thread forms each step from the sessions that
  * have a frame waiting (one frame per session per step, oldest first, round
- * robin), launches it through a batch runner while the previous step is still
- * on the GPU (two steps in flight), and a completion thread timestamps each
- * frame's result.  Every session's volume, pose and maps stay on the device
+ * robin) and launches it through one of `lanes` batch runners, each on its
+ * own stream, so several steps run on the GPU at once (by default three, one
+ * step per lane); a completion thread per lane timestamps each frame's
+ * result.  Every session's volume, pose and maps stay on the device
  * between frames.  Sessions are admitted while the resident set fits the HBM
  * budget (vs_session_bytes of each) and a resident slot is free; a session
  * that does not fit yet waits, queues its frames, and is admitted when closed
@@ -435,7 +436,11 @@ typedef struct {
   int max_resident;         /* resident sessions, 1..VS_MAX_BATCH (0: VS_MAX_BATCH) */
   int max_batch;            /* sessions per step, 1..VS_MAX_BATCH (0: VS_MAX_BATCH) */
   int queue_depth;          /* frames buffered per session, 1..256 (0: 8)    */
-  int pipeline;             /* steps in flight, 1..2 (0: 2)                  */
+  int pipeline;             /* steps in flight per lane, 1..2 (0: 1)         */
+  int lanes;                /* steps run at the same time, each on its own
+                               stream and batch runner, 1..4 (0: 3); with
+                               more than one, a session joins a step only
+                               when none of its frames is in flight        */
 } vs_server_config;
 
 typedef struct {

@@ -52,9 +52,12 @@ def _collect(srv, want, timeout_s=60.0):
     return got
 
 
-def test_serving_equals_alone_in_a_random_mix(cases, alone):
+@pytest.mark.parametrize("lanes,pipeline", [(1, 2), (2, 1), (3, 2)])
+def test_serving_equals_alone_in_a_random_mix(cases, alone, lanes, pipeline):
+    """one lane, or several lanes whose steps run at the same time on their
+    own streams: the same per-frame poses and final volumes"""
     rng = np.random.default_rng(5)
-    with V.Server() as srv:
+    with V.Server(lanes=lanes, pipeline=pipeline) as srv:
         ids = [srv.open(c["cfg"]) for c in cases]
         assert all(srv.state(i) == V.VS_SESSION_RESIDENT for i in ids)
         order = [i for i in range(len(cases)) for _ in range(FRAMES)]

@@ -5,16 +5,19 @@
 // session's pinned ring (queue_depth frames) and stamped with its arrival
 // time.  A worker thread forms a step from the sessions that have a frame not
 // yet launched (round robin, one frame per session, at most max_batch) and
-// launches it through the batch runner; it keeps up to `pipeline` steps in
-// flight, so the host prepares and enqueues step k+1 while step k runs and
-// the GPU does not idle between steps.  A completion thread waits for the
-// steps in order, stamps each frame's result, releases its ring slot and
-// retires closed sessions.
+// launches it through a batch runner.  There are `lanes` runners, each on its
+// own stream with its own completion thread: steps of different lanes run on
+// the GPU at the same time, so one step's latency-bound phases (ICP closes,
+// kernel tails) overlap another step's work.  A lane keeps up to `pipeline`
+// steps in flight, so the host prepares and enqueues step k+1 while step k
+// runs.  A lane's completion thread waits for its steps in order, stamps each
+// frame's result, releases its ring slot and retires closed sessions.
 //
 // Ring of a session: frames [head, sent) are on the GPU, [sent, tail) wait
 // for a step, slots of frames before head are free.  A session's frames run
-// in submission order because its frame k+1 can only join a step launched
-// after the step holding frame k, on the same stream.
+// in submission order: with one lane its frame k+1 can only join a step
+// launched after the step holding frame k, on the same stream; with several
+// lanes a session joins a step only when none of its frames is in flight.
 //
 // Admission.  A session is resident (volume, pose, pyramid and maps on the
 // device) while it is open.  It is admitted when a resident slot is free and
@@ -59,6 +62,8 @@ struct SrvSession {
   uint64_t head = 0, sent = 0, tail = 0;
 };
 
+constexpr int kMaxLanes = 4;
+
 struct StepRec {
   int ring = 0;
   int n = 0;
@@ -72,12 +77,12 @@ struct StepRec {
 struct vs_server {
   vs_server_config cfg;
   int device = 0;
-  vs_batch* batch = nullptr;
+  vs_batch* batch[kMaxLanes] = {};
   std::mutex mu;
   std::condition_variable cv_work, cv_done, cv_res;
   std::map<int, SrvSession*> sessions;
   std::deque<int> waiting;
-  std::deque<StepRec> inflight;
+  std::deque<StepRec> inflight[kMaxLanes];
   std::deque<vs_result> results;
   int next_id = 0;
   int rr = 0;
@@ -89,7 +94,7 @@ struct vs_server {
   bool stop = false;
   int error = 0;
   std::string error_msg;
-  std::thread worker, completer;
+  std::thread worker, completer[kMaxLanes];
 };
 
 namespace {
@@ -157,12 +162,25 @@ bool any_admissible(const vs_server* s) {
   return false;
 }
 
+// a frame the worker may put into a step: waiting, and with several lanes
+// none of the session's frames still in flight
+bool ready(const vs_server* s, const SrvSession* r) {
+  return r->state == VS_SESSION_RESIDENT && r->sent < r->tail && (s->cfg.lanes == 1 || r->sent == r->head);
+}
+
 bool any_ready(const vs_server* s) {
-  for (const auto& kv : s->sessions) {
-    const SrvSession* r = kv.second;
-    if (r->state == VS_SESSION_RESIDENT && r->sent < r->tail) return true;
-  }
+  for (const auto& kv : s->sessions)
+    if (ready(s, kv.second)) return true;
   return false;
+}
+
+// the lane with the fewest steps in flight, or -1 when every lane is full
+int free_lane(const vs_server* s) {
+  int best = -1;
+  for (int l = 0; l < s->cfg.lanes; l++)
+    if ((int)s->inflight[l].size() < s->cfg.pipeline && (best < 0 || s->inflight[l].size() < s->inflight[best].size()))
+      best = l;
+  return best;
 }
 
 void worker_main(vs_server* s) {
@@ -172,11 +190,11 @@ void worker_main(vs_server* s) {
   for (;;) {
     admit(s, lk);
     s->cv_work.wait(lk, [&] {
-      return s->stop || s->error || any_admissible(s) ||
-             ((int)s->inflight.size() < s->cfg.pipeline && any_ready(s));
+      return s->stop || s->error || any_admissible(s) || (free_lane(s) >= 0 && any_ready(s));
     });
     if (s->stop || s->error) return;
-    if ((int)s->inflight.size() >= s->cfg.pipeline || !any_ready(s)) continue;
+    const int lane = free_lane(s);
+    if (lane < 0 || !any_ready(s)) continue;
     // round robin over the resident sessions, one frame each
     order.clear();
     for (const auto& kv : s->sessions) order.push_back(kv.second);
@@ -188,7 +206,7 @@ void worker_main(vs_server* s) {
     for (int j = 0; j < m && rec.n < s->cfg.max_batch; j++) {
       const int idx = (s->rr + j) % m;
       SrvSession* r = order[idx];
-      if (r->state != VS_SESSION_RESIDENT || r->sent >= r->tail) continue;
+      if (!ready(s, r)) continue;
       const size_t slot = r->sent % (uint64_t)s->cfg.queue_depth;
       rec.ids[rec.n] = r->id;
       rec.frame[rec.n] = r->sent;
@@ -202,7 +220,7 @@ void worker_main(vs_server* s) {
     s->rr = m ? last % m : 0;
     lk.unlock();
     int ring = 0;
-    const int rc = batch_launch_host(s->batch, ss, rec.n, fp, &ring);
+    const int rc = batch_launch_host(s->batch[lane], ss, rec.n, fp, &ring);
     const std::string msg = rc ? vs_last_error() : "";
     lk.lock();
     if (rc) {
@@ -210,7 +228,7 @@ void worker_main(vs_server* s) {
       return;
     }
     rec.ring = ring;
-    s->inflight.push_back(rec);
+    s->inflight[lane].push_back(rec);
     s->steps += 1;
     s->batch_sum += rec.n;
     if (rec.n > s->max_batch_seen) s->max_batch_seen = rec.n;
@@ -232,21 +250,22 @@ void retire(vs_server* s, SrvSession* r, std::unique_lock<std::mutex>& lk) {
   s->cv_work.notify_all();
 }
 
-void completer_main(vs_server* s) {
+void completer_main(vs_server* s, int lane) {
   cudaSetDevice(s->device);
   std::unique_lock<std::mutex> lk(s->mu);
+  std::deque<StepRec>& q = s->inflight[lane];
   for (;;) {
-    s->cv_done.wait(lk, [&] { return s->stop || s->error || !s->inflight.empty(); });
-    if (s->inflight.empty() || s->error) {
+    s->cv_done.wait(lk, [&] { return s->stop || s->error || !q.empty(); });
+    if (q.empty() || s->error) {
       if (s->stop || s->error) return;
       continue;
     }
-    const StepRec rec = s->inflight.front();
+    const StepRec rec = q.front();
     lk.unlock();
-    const cudaError_t e = cudaEventSynchronize(batch_done(s->batch, rec.ring));
+    const cudaError_t e = cudaEventSynchronize(batch_done(s->batch[lane], rec.ring));
     const double t = now_s();
     std::vector<vs_result> out(rec.n);
-    const unsigned char* heads = batch_heads(s->batch, rec.ring);
+    const unsigned char* heads = batch_heads(s->batch[lane], rec.ring);
     for (int i = 0; i < rec.n; i++) {
       const Pose* p = reinterpret_cast<const Pose*>(heads + (size_t)i * kPoseHeadBytes);
       vs_result& o = out[i];
@@ -264,7 +283,7 @@ void completer_main(vs_server* s) {
       set_server_error(s, VS_ERR_CUDA, std::string("step: ") + cudaGetErrorString(e));
       return;
     }
-    s->inflight.pop_front();
+    q.pop_front();
     for (int i = 0; i < rec.n; i++) {
       SrvSession* r = s->sessions[rec.ids[i]];
       r->head += 1;
@@ -299,7 +318,8 @@ void vs_server_config_default(vs_server_config* c) {
   c->max_resident = kMaxSlots;
   c->max_batch = kMaxSlots;
   c->queue_depth = 8;
-  c->pipeline = 2;
+  c->pipeline = 1;
+  c->lanes = 3;
 }
 
 int vs_server_create(const vs_server_config* c, vs_server** out) {
@@ -313,20 +333,25 @@ int vs_server_create(const vs_server_config* c, vs_server** out) {
     if (c->max_batch) k.max_batch = c->max_batch;
     if (c->queue_depth) k.queue_depth = c->queue_depth;
     if (c->pipeline) k.pipeline = c->pipeline;
+    if (c->lanes) k.lanes = c->lanes;
   }
   if (k.max_resident < 1 || k.max_resident > kMaxSlots || k.max_batch < 1 || k.max_batch > kMaxSlots ||
-      k.queue_depth < 1 || k.queue_depth > 256 || k.pipeline < 1 || k.pipeline > 2)
+      k.queue_depth < 1 || k.queue_depth > 256 || k.pipeline < 1 || k.pipeline > 2 || k.lanes < 1 ||
+      k.lanes > kMaxLanes)
     return fail_code(VS_ERR_ARG, "server config out of range");
   vs_server* s = new vs_server;
   s->cfg = k;
   cudaGetDevice(&s->device);
-  int rc = vs_batch_create(&s->batch);
-  if (rc) {
-    delete s;
-    return rc;
+  for (int l = 0; l < k.lanes; l++) {
+    const int rc = vs_batch_create(&s->batch[l]);
+    if (rc) {
+      for (int m = 0; m < l; m++) vs_batch_destroy(s->batch[m]);
+      delete s;
+      return rc;
+    }
   }
   s->worker = std::thread(worker_main, s);
-  s->completer = std::thread(completer_main, s);
+  for (int l = 0; l < k.lanes; l++) s->completer[l] = std::thread(completer_main, s, l);
   *out = s;
   return VS_OK;
 }
@@ -482,11 +507,12 @@ int vs_server_destroy(vs_server* s) {
   s->cv_done.notify_all();
   s->cv_res.notify_all();
   if (s->worker.joinable()) s->worker.join();
-  if (s->completer.joinable()) s->completer.join();
-  vs_batch_sync(s->batch);
+  for (int l = 0; l < s->cfg.lanes; l++)
+    if (s->completer[l].joinable()) s->completer[l].join();
+  for (int l = 0; l < s->cfg.lanes; l++) vs_batch_sync(s->batch[l]);
   for (auto& kv : s->sessions) free_record(kv.second);
   s->sessions.clear();
-  vs_batch_destroy(s->batch);
+  for (int l = 0; l < s->cfg.lanes; l++) vs_batch_destroy(s->batch[l]);
   delete s;
   return VS_OK;
 }

@@ -86,6 +86,7 @@ class ServerConfig(ctypes.Structure):
         ("max_batch", ctypes.c_int),
         ("queue_depth", ctypes.c_int),
         ("pipeline", ctypes.c_int),
+        ("lanes", ctypes.c_int),
     ]
 
 
@@ -640,12 +641,12 @@ class Server:
     """Serving loop: continuous batching of frames from many sessions with
     admission by HBM budget (vs_server_* in include/vs.h)."""
 
-    def __init__(self, hbm_budget=0, max_resident=0, max_batch=0, queue_depth=0, pipeline=0):
+    def __init__(self, hbm_budget=0, max_resident=0, max_batch=0, queue_depth=0, pipeline=0, lanes=0):
         self.lib = load()
         c = ServerConfig()
         self.lib.vs_server_config_default(ctypes.byref(c))
         for k, v in dict(hbm_budget=hbm_budget, max_resident=max_resident, max_batch=max_batch,
-                         queue_depth=queue_depth, pipeline=pipeline).items():
+                         queue_depth=queue_depth, pipeline=pipeline, lanes=lanes).items():
             if v:
                 setattr(c, k, v)
         h = ctypes.c_void_p()
