@@ -564,7 +564,8 @@ def run_ours(args):
     if not args.no_autotune:
         shape, ms = batch.autotune(warm, reps=3)
         tuned = {"ray_tile": "%dx%d" % (1 << shape[0], 32 >> shape[0]), "march_blocks_per_sm": shape[1],
-                 "shade_blocks_per_sm": shape[2], "raycast_ms_warm_sessions": ms}
+                 "shade_blocks_per_sm": shape[2], "bilateral_tile": "32x%d" % shape[3],
+                 "integrate_blocks_per_sm": shape[4] or "all resident", "raycast_ms_warm_sessions": ms}
     for w in warm:
         w.close()
 

@@ -398,22 +398,29 @@ int vs_batch_get_stage_times(vs_batch* b, float* ms);
 /* kernels one step launches (the same for every batch size) */
 int vs_batch_kernels_per_step(vs_batch* b);
 
-/* Launch shape of the ray-cast kernels of a runner's steps: a warp's 32 rays
- * form a (1 << ray_tile_log2) x (32 >> ray_tile_log2) pixel tile, and the
- * march / shading grids hold that many 128-thread blocks per SM (0: as many
- * as fit).  The shape changes no result, only time. */
+/* Launch shape of a runner's steps: a warp's 32 rays form a
+ * (1 << ray_tile_log2) x (32 >> ray_tile_log2) pixel tile, and the march /
+ * shading grids hold that many 128-thread blocks per SM (0: as many as fit);
+ * the bilateral filter and the sub-cube activation work on 32 x
+ * bilateral_rows pixel tiles (4, 8 or 16; 0: 8); the integration's update
+ * grid holds integrate_blocks_per_sm 256-thread blocks per SM (0: as many as
+ * fit).  The shape changes no result, only time. */
 typedef struct {
   int ray_tile_log2;        /* 0..5, default 3 (8 x 4 rays)                  */
   int march_blocks_per_sm;
   int shade_blocks_per_sm;
+  int bilateral_rows;
+  int integrate_blocks_per_sm;
 } vs_launch_shape;
 
 int vs_batch_get_launch_shape(vs_batch* b, vs_launch_shape* out);
 int vs_batch_set_launch_shape(vs_batch* b, const vs_launch_shape* in);
-/* Autotuner: times the ray-cast stage of these sessions (their current
- * volumes and poses; no state changes) under every candidate shape, reps
- * launches each, and keeps the fastest for the runner's later steps.  best and
- * best_ms (ms per ray-cast stage) may be NULL. */
+/* Autotuner: times three stages of these sessions (their current frames,
+ * volumes and poses; no state changes) under their candidate shapes, reps
+ * launches each, and keeps the fastest of each for the runner's later steps:
+ * the ray-cast (ray tile and march grid), the filter (tile rows) and the
+ * integration (update grid, timed as dry runs that store no voxel).  best
+ * and best_ms (ms per ray-cast stage) may be NULL. */
 int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps, vs_launch_shape* best,
                       float* best_ms);
 

@@ -1,10 +1,12 @@
 """Launch-shape autotuner of the batch runner (vs_batch_autotune).
 
 A launch shape (how a warp's 32 rays are tiled, how many blocks per SM the
-ray-cast grids hold) changes only time: every shape must give bit-identical
-poses, volumes and maps, the tuner must leave every session's state as it was
-(it re-runs the ray-cast on the current volume and pose), and a tuned runner
-must continue the sequence exactly as an untuned one."""
+ray-cast grids hold, the rows of the filter / activation tile, the update
+grid of the integration) changes only time: every shape must give
+bit-identical poses, volumes and maps, the tuner must leave every session's
+state as it was (it re-runs the ray-cast and the filter on the current data
+and the integration as a dry run), and a tuned runner must continue the
+sequence exactly as an untuned one."""
 import numpy as np
 import pytest
 
@@ -50,6 +52,8 @@ def _run(cases, shape=None, tune_after=None):
                 before = [_snapshot(s) for s in ss]
                 best, ms = b.autotune(ss, reps=2)
                 assert 1 <= best[0] <= 5 and best[1] >= 1 and ms > 0
+                assert best[3] in (4, 8, 16) and best[4] in (0, 2, 3)
+                assert b.launch_shape() == best
                 for s, snap in zip(ss, before):
                     _same(_snapshot(s), snap, "state after autotune")
         snaps = [_snapshot(s) for s in ss]
@@ -60,7 +64,7 @@ def _run(cases, shape=None, tune_after=None):
 
 def test_every_launch_shape_gives_the_same_results(cases):
     ref = _run(cases)
-    for shape in [(5, 4, 0), (1, 0, 3), (4, 2, 2)]:
+    for shape in [(5, 4, 0), (1, 0, 3), (4, 2, 2), (3, 0, 0, 4, 2), (2, 0, 0, 16, 3)]:
         got = _run(cases, shape=shape)
         for i, (a, b) in enumerate(zip(ref, got)):
             _same(a, b, "shape %s session %d" % (shape, i))
@@ -79,3 +83,6 @@ def test_launch_shape_rejects_out_of_range(cases):
             b.set_launch_shape(6)
         assert e.value.code == V.VS_ERR_ARG
         assert b.launch_shape()[0] == 3
+        for bad in [(3, 0, 0, 5, 0), (3, 0, 0, 8, 33)]:
+            with pytest.raises(V.VsError):
+                b.set_launch_shape(*bad)

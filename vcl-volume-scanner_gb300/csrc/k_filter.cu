@@ -18,19 +18,21 @@
 namespace vs {
 namespace {
 
-constexpr int BX = 32, BY = 8;  // output tile of the bilateral filter
+constexpr int BX = 32, BY = 8;  // output tile of the bilateral filter (BY: default rows; 4 and 16 also built)
 constexpr int kScanSmem = 64 * 1024;  // staged normal-rejection bitmasks of one level
 
 // The reference reads a linear-filtered texture at integer coordinates, so
 // every tap is the mean of the 2x2 texels (X-1..X, Y-1..Y); out-of-range texel
 // coordinates clamp to the edge.  A tile of BX x BY outputs needs taps
 // X in [x0-2, x0+BX+1] and texels in [x0-3, x0+BX+1].
+template <int R>
 struct BilateralSmem {
-  float tex[BY + 5][BX + 6];
-  float tap[BY + 4][BX + 5];
+  float tex[R + 5][BX + 6];
+  float tap[R + 4][BX + 5];
 };
 
-__device__ inline float bilateral_px(const BilateralSmem& m, int tx, int ty, const float g[5]) {
+template <int R>
+__device__ inline float bilateral_px(const BilateralSmem<R>& m, int tx, int ty, const float g[5]) {
   const float denom = 2.0f * 0.1f * 0.1f;  // 2 sigma_r^2, sigma_r = 0.1 m (z_yooji_cuda_img_proc.cu:44,91)
   const float center = m.tap[ty + 2][tx + 2];
   float t = 0.0f, sum = 0.0f;
@@ -49,14 +51,14 @@ __device__ inline float bilateral_px(const BilateralSmem& m, int tx, int ty, con
   return t / sum;
 }
 
-// one BX x BY output tile; the block's threads all take part (two barriers)
-template <bool FROM_MM>
-__device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restrict__ mm,
+// one BX x R output tile; the block's BX x R threads all take part (two barriers)
+template <bool FROM_MM, int R>
+__device__ inline void bilateral_tile(BilateralSmem<R>& m, const uint16_t* __restrict__ mm,
                                       const float* __restrict__ fin, float scale, float* __restrict__ raw_out,
                                       float* __restrict__ out, int W, int H, int x0, int y0, const float g[5],
                                       float2* __restrict__ dl_out = nullptr, const float* __restrict__ lam = nullptr) {
   const int tid = threadIdx.y * BX + threadIdx.x;
-  for (int i = tid; i < (BY + 5) * (BX + 5); i += BX * BY) {
+  for (int i = tid; i < (R + 5) * (BX + 5); i += BX * R) {
     int ty = i / (BX + 5), tx = i - ty * (BX + 5);
     int gx = min(max(x0 - 3 + tx, 0), W - 1);
     int gy = min(max(y0 - 3 + ty, 0), H - 1);
@@ -68,7 +70,7 @@ __device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restri
     m.tex[ty][tx] = v;
   }
   __syncthreads();
-  for (int i = tid; i < (BY + 4) * (BX + 4); i += BX * BY) {
+  for (int i = tid; i < (R + 4) * (BX + 4); i += BX * R) {
     int ty = i / (BX + 4), tx = i - ty * (BX + 4);
     m.tap[ty][tx] = 0.25f * ((m.tex[ty][tx] + m.tex[ty][tx + 1]) + (m.tex[ty + 1][tx] + m.tex[ty + 1][tx + 1]));
   }
@@ -85,8 +87,9 @@ __device__ inline void bilateral_tile(BilateralSmem& m, const uint16_t* __restri
   }
 }
 
-__global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __restrict__ bt) {
-  __shared__ BilateralSmem m;
+template <int R>
+__global__ void __launch_bounds__(BX* R) k_bilateral_batch(const BatchTable* __restrict__ bt) {
+  __shared__ BilateralSmem<R> m;
   const int n = bt->n;
   const int total = bt->bil[n];
   for (int item = blockIdx.x; item < total; item += gridDim.x) {
@@ -96,11 +99,11 @@ __global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __
     const int W = s->lv[0].W, H = s->lv[0].H;
     const int tw = (W + BX - 1) / BX;
     const float g[5] = {s->gauss[0], s->gauss[1], s->gauss[2], s->gauss[1], s->gauss[0]};
-    bilateral_tile<true>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
-                         (t / tw) * BY, g, s->lam_map ? s->dl_map : nullptr, s->lam_map);
+    bilateral_tile<true, R>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
+                            (t / tw) * R, g, s->lam_map ? s->dl_map : nullptr, s->lam_map);
     if (s->rgb_packed) {
       // the colour frame as one word per pixel, for the integration's gathers
-      const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * BY + threadIdx.y;
+      const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * R + threadIdx.y;
       if (x < W && y < H) {
         const size_t i = (size_t)y * W + x, plane = (size_t)W * H;
         s->rgb_packed[i] = pack_rgb(s->rgb_in[i], s->rgb_in[plane + i], s->rgb_in[2 * plane + i]);
@@ -113,9 +116,9 @@ __global__ void __launch_bounds__(BX* BY) k_bilateral_batch(const BatchTable* __
 __global__ void __launch_bounds__(BX* BY)
     k_bilateral_float(const float* __restrict__ in, float* __restrict__ out, int W, int H, float g0, float g1,
                       float g2) {
-  __shared__ BilateralSmem m;
+  __shared__ BilateralSmem<BY> m;
   const float g[5] = {g0, g1, g2, g1, g0};
-  bilateral_tile<false>(m, nullptr, in, 1.0f, nullptr, out, W, H, blockIdx.x * BX, blockIdx.y * BY, g);
+  bilateral_tile<false, BY>(m, nullptr, in, 1.0f, nullptr, out, W, H, blockIdx.x * BX, blockIdx.y * BY, g);
 }
 
 // level l -> l+1: separable [1 4 6 4 1] smoothing (borders 0, no validity
@@ -364,9 +367,19 @@ __global__ void __launch_bounds__(256) k_inmap_post(const BatchTable* __restrict
 
 }  // namespace
 
-void launch_filter(const BatchTable* bt, cudaStream_t st) {
+void launch_filter(const BatchTable* bt, cudaStream_t st, int rows) {
   const int grid = sm_count() * 8;
-  k_bilateral_batch<<<grid, dim3(BX, BY), 0, st>>>(bt);
+  switch (rows) {
+    case 4:
+      k_bilateral_batch<4><<<grid * 2, dim3(BX, 4), 0, st>>>(bt);
+      break;
+    case 16:
+      k_bilateral_batch<16><<<grid / 2, dim3(BX, 16), 0, st>>>(bt);
+      break;
+    default:
+      k_bilateral_batch<BY><<<grid, dim3(BX, BY), 0, st>>>(bt);
+      break;
+  }
   for (int l = 1; l < kMaxLevels; l++) k_pyramid_batch<<<grid, dim3(32, 8), 0, st>>>(bt, l);
 }
 
@@ -390,10 +403,11 @@ void configure_filter_kernels() {
 // work-item prefixes of a batch; host_recs are the host copies of the
 // session records, dev_recs their device addresses
 void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n,
-                      int ray_lx) {
+                      int ray_lx, int bil_rows) {
   std::memset(&hb, 0, sizeof(hb));
   hb.n = n;
   hb.ray_lx = ray_lx;
+  hb.bil_rows = (bil_rows == 4 || bil_rows == 16) ? bil_rows : BY;
   const int rx = 1 << ray_lx, ry = 32 >> ray_lx;
   for (int i = 0; i < n; i++) {
     const SessionDev& h = *host_recs[i];
@@ -406,7 +420,7 @@ void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const 
       ipost += ((w + 15) / 16) * ((hh + 15) / 16);
       ray += ((w + rx - 1) / rx) * ((hh + ry - 1) / ry);
     }
-    hb.bil[i + 1] = hb.bil[i] + ((h.lv[0].W + BX - 1) / BX) * ((h.lv[0].H + BY - 1) / BY);
+    hb.bil[i + 1] = hb.bil[i] + ((h.lv[0].W + BX - 1) / BX) * ((h.lv[0].H + hb.bil_rows - 1) / hb.bil_rows);
     for (int l = 1; l < kMaxLevels; l++)
       hb.pyr[l - 1][i + 1] =
           hb.pyr[l - 1][i] + (l < h.levels ? ((h.lv[l].W + 31) / 32) * ((h.lv[l].H + 7) / 8) : 0);

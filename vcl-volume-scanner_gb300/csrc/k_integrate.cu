@@ -97,38 +97,41 @@ __global__ void __launch_bounds__(256) k_activate(const BatchTable* __restrict__
     if (gate && s->pose->failed) continue;
     const int W = s->lv[0].W, H = s->lv[0].H;
     const int tw = (W + 31) / 32;
-    const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * 8 + threadIdx.y;
-    if (x >= W || y >= H) continue;
-    const float* depth = depth_ext ? depth_ext : s->depth_raw;
-    const float td = depth[(size_t)y * W + x];
-    if (!(td > 0.0f)) continue;
-    const float* Tcg_in = Tcg_ext ? Tcg_ext : s->pose->Tcg;
-    float T[12];
-#pragma unroll
-    for (int k = 0; k < 12; k++) T[k] = Tcg_in[k];
-    const float* K = s->lv[0].K;
-    F3 p = transform(back_project((float)x, (float)y, K, td), T);
-    F3 pe = transform(back_project((float)x, (float)y, K, 100.0f), T);
-    F3 dv = normalised(sub(pe, p));
-    const int nb0 = s->nb[0], nb1 = s->nb[1], nb2 = s->nb[2];
-    const uint32_t stamp = s->brick_count[2];
-    int prev = -1;
-    for (int m = -4; m <= 1; m++) {
-      F3 tp = add(p, scale(((float)m) * s->mu, dv));
-      F3 v;
-      if (!pos_in_voxel(tp, *s, v)) continue;
-      int xs = roundf_div8_ref(v.x), ys = roundf_div8_ref(v.y), zs = roundf_div8_ref(v.z);
-      if (xs < 0 || xs >= nb0 || ys < 0 || ys >= nb1 || zs < 0 || zs >= nb2) break;
-      int b = (zs * nb1 + ys) * nb0 + xs;
-      if (b == prev) continue;
-      prev = b;
-      // an L1-cached read of the flag may be stale, but only ever with an
-      // older stamp, and the exchange then decides: it returns the current
-      // stamp to every thread but the first
-      uint32_t* f = s->brick_flag + b;
-      if (*f != stamp && atomicExch(f, stamp) != stamp) {
-        uint32_t pos = atomicAdd(s->brick_count, 1u);
-        s->brick_list[pos] = (uint32_t)b;
+    const int rows = bt->bil_rows;
+    for (int ty = threadIdx.y; ty < rows; ty += blockDim.y) {
+      const int x = (t % tw) * 32 + threadIdx.x, y = (t / tw) * rows + ty;
+      if (x >= W || y >= H) continue;
+      const float* depth = depth_ext ? depth_ext : s->depth_raw;
+      const float td = depth[(size_t)y * W + x];
+      if (!(td > 0.0f)) continue;
+      const float* Tcg_in = Tcg_ext ? Tcg_ext : s->pose->Tcg;
+      float T[12];
+  #pragma unroll
+      for (int k = 0; k < 12; k++) T[k] = Tcg_in[k];
+      const float* K = s->lv[0].K;
+      F3 p = transform(back_project((float)x, (float)y, K, td), T);
+      F3 pe = transform(back_project((float)x, (float)y, K, 100.0f), T);
+      F3 dv = normalised(sub(pe, p));
+      const int nb0 = s->nb[0], nb1 = s->nb[1], nb2 = s->nb[2];
+      const uint32_t stamp = s->brick_count[2];
+      int prev = -1;
+      for (int m = -4; m <= 1; m++) {
+        F3 tp = add(p, scale(((float)m) * s->mu, dv));
+        F3 v;
+        if (!pos_in_voxel(tp, *s, v)) continue;
+        int xs = roundf_div8_ref(v.x), ys = roundf_div8_ref(v.y), zs = roundf_div8_ref(v.z);
+        if (xs < 0 || xs >= nb0 || ys < 0 || ys >= nb1 || zs < 0 || zs >= nb2) break;
+        int b = (zs * nb1 + ys) * nb0 + xs;
+        if (b == prev) continue;
+        prev = b;
+        // an L1-cached read of the flag may be stale, but only ever with an
+        // older stamp, and the exchange then decides: it returns the current
+        // stamp to every thread but the first
+        uint32_t* f = s->brick_flag + b;
+        if (*f != stamp && atomicExch(f, stamp) != stamp) {
+          uint32_t pos = atomicAdd(s->brick_count, 1u);
+          s->brick_list[pos] = (uint32_t)b;
+        }
       }
     }
   }
@@ -386,7 +389,7 @@ __device__ __forceinline__ void nearest_pixel(float x, float y, float z, const f
 template <class S, bool COLOR>
 __global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
     k_integrate(const BatchTable* __restrict__ bt, const float* __restrict__ depth_ext,
-                const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext, int color) {
+                const float* __restrict__ Tgc_ext, const float* __restrict__ Tcg_ext, int color, int dry) {
   __shared__ uint32_t pre[kMaxSlots + 1];  // prefix of the slots' active-brick counts
   // per thread, per x value of its voxels: the transform rows' partial sums
   // M0 x + M1 y, M4 x + M5 y, M8 x + M9 y and (x - Cx)^2 + (y - Cy)^2
@@ -569,11 +572,11 @@ __global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
         upd |= 1u << j;
         nupd++;
       }
-      if (COLOR && q.col && upd)
+      if (COLOR && q.col && upd && !dry)
         color_round<S, kPerVec, kRound>(q, upd, r * kRound, lane, bx, by, bz, b, wv, lx, ly, lz);
 #pragma unroll
       for (int v = 0; v < kRV; v++)
-        if (changed[v]) {
+        if (changed[v] && !dry) {
           memcpy(&cur[v], wv[v], 16);
           bv[(r * kRV + v) * 32 + lane] = cur[v];
         }
@@ -747,11 +750,13 @@ int resident_blocks() {
 
 template <class S>
 void launch_update(const BatchTable* bt, const float* depth, const float* Tgc, const float* Tcg, bool color,
-                   cudaStream_t st) {
+                   cudaStream_t st, int blocks_per_sm, bool dry) {
+  const int most = color ? resident_blocks<S, true>() : resident_blocks<S, false>();
+  const int grid = (blocks_per_sm > 0 && blocks_per_sm * sm_count() < most) ? blocks_per_sm * sm_count() : most;
   if (color)
-    k_integrate<S, true><<<resident_blocks<S, true>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 1);
+    k_integrate<S, true><<<grid, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 1, dry ? 1 : 0);
   else
-    k_integrate<S, false><<<resident_blocks<S, false>(), kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 0);
+    k_integrate<S, false><<<grid, kIntThreads, 0, st>>>(bt, depth, Tgc, Tcg, 0, dry ? 1 : 0);
 }
 
 void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) {
@@ -761,20 +766,20 @@ void launch_session_tables(const SessionDev& h, SessionDev* d, cudaStream_t st) 
 }
 
 void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc, const float* Tcg,
-                      bool gate, cudaStream_t st, bool color) {
+                      bool gate, cudaStream_t st, bool color, int blocks_per_sm, bool dry) {
   const int c = color ? 1 : 0;
   k_integrate_prepare<<<1, kMaxSlots, 0, st>>>(bt, gate ? 1 : 0);
   k_activate<<<sm_count() * 8, dim3(32, 8), 0, st>>>(bt, depth, Tcg, gate ? 1 : 0);
   // persistent grid: every block resident at once
   switch (tsdf_type) {
     case VS_TSDF_FP16:
-      launch_update<StoreF16>(bt, depth, Tgc, Tcg, c != 0, st);
+      launch_update<StoreF16>(bt, depth, Tgc, Tcg, c != 0, st, blocks_per_sm, dry);
       break;
     case VS_TSDF_FP32:
-      launch_update<StoreF32>(bt, depth, Tgc, Tcg, c != 0, st);
+      launch_update<StoreF32>(bt, depth, Tgc, Tcg, c != 0, st, blocks_per_sm, dry);
       break;
     default:
-      launch_update<StoreI16>(bt, depth, Tgc, Tcg, c != 0, st);
+      launch_update<StoreI16>(bt, depth, Tgc, Tcg, c != 0, st, blocks_per_sm, dry);
       break;
   }
 }

@@ -28,6 +28,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <functional>
 #include <cstring>
 #include <string>
 
@@ -97,10 +98,10 @@ void drop_graphs(vs_batch* b) {
 // one group's per-frame chain on one stream
 void record_chain(vs_batch* b, const BatchTable* t, cudaStream_t st) {
   const Schedule& k = b->sched;
-  launch_filter(t, st);
+  launch_filter(t, st, b->shape.bil_rows);
   if (k.inmaps) launch_input_maps(t, st);
   launch_icp(t, k.levels, k.iters, k.reduce_mode, st, true, nullptr);
-  launch_integrate(t, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
+  launch_integrate(t, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0, b->shape.integrate_blocks_per_sm);
   launch_raycast(t, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr, nullptr,
                  nullptr, st, b->shape, nullptr, k.color != 0);
 }
@@ -126,7 +127,7 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
     // stage timing: the stages one after another (ICP still on branches), so
     // that each stage's time is its own
     mark(0);
-    launch_filter(b->d_tab, st);
+    launch_filter(b->d_tab, st, b->shape.bil_rows);
     if (k.inmaps) launch_input_maps(b->d_tab, st);
     mark(1);
     cudaEventRecord(b->fork, st);
@@ -138,7 +139,8 @@ void record_step(vs_batch* b, int r, cudaStream_t st) {
       cudaStreamWaitEvent(st, b->join[g], 0);
     }
     mark(2);
-    launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0);
+    launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, st, k.color != 0,
+                     b->shape.integrate_blocks_per_sm);
     mark(3);
     launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr, nullptr,
                    nullptr, nullptr, st, b->shape, nullptr, k.color != 0);
@@ -227,7 +229,7 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
     hr[i] = &ss[i]->h;
     dr[i] = ss[i]->d;
   }
-  fill_batch_table(*b->h_tab[r], hr, dr, n, b->shape.ray_lx);
+  fill_batch_table(*b->h_tab[r], hr, dr, n, b->shape.ray_lx, b->shape.bil_rows);
   // ICP groups: largest sessions first, each to the group with fewer pixels
   int order[kMaxSlots];
   for (int i = 0; i < n; i++) order[i] = i;
@@ -247,7 +249,8 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
     gn[g]++;
     load[g] += px(i);
   }
-  for (int g = 0; g < kIcpGroups; g++) fill_batch_table(b->h_grp[r][g], gh[g], gd[g], gn[g], b->shape.ray_lx);
+  for (int g = 0; g < kIcpGroups; g++)
+    fill_batch_table(b->h_grp[r][g], gh[g], gd[g], gn[g], b->shape.ray_lx, b->shape.bil_rows);
   cudaError_t e = cudaGraphLaunch(b->exec[r], st);
   if (e == cudaSuccess) e = cudaEventRecord(b->done[r], st);
   if (e != cudaSuccess) return cuda_fail_code(e, "batch step launch");
@@ -455,27 +458,56 @@ int vs_batch_get_launch_shape(vs_batch* b, vs_launch_shape* out) {
   out->ray_tile_log2 = b->shape.ray_lx;
   out->march_blocks_per_sm = b->shape.march_blocks_per_sm;
   out->shade_blocks_per_sm = b->shape.shade_blocks_per_sm;
+  out->bilateral_rows = b->shape.bil_rows;
+  out->integrate_blocks_per_sm = b->shape.integrate_blocks_per_sm;
   return VS_OK;
 }
 
 int vs_batch_set_launch_shape(vs_batch* b, const vs_launch_shape* in) {
   if (!b || !in) return fail_code(VS_ERR_ARG, "null argument");
   if (in->ray_tile_log2 < 0 || in->ray_tile_log2 > 5 || in->march_blocks_per_sm < 0 || in->shade_blocks_per_sm < 0 ||
-      in->march_blocks_per_sm > 32 || in->shade_blocks_per_sm > 32)
+      in->march_blocks_per_sm > 32 || in->shade_blocks_per_sm > 32 || in->integrate_blocks_per_sm < 0 ||
+      in->integrate_blocks_per_sm > 32 ||
+      (in->bilateral_rows != 0 && in->bilateral_rows != 4 && in->bilateral_rows != 8 && in->bilateral_rows != 16))
     return fail_code(VS_ERR_ARG, "launch shape out of range");
   int rc = vs_batch_sync(b);
   if (rc) return rc;
   b->shape.ray_lx = in->ray_tile_log2;
   b->shape.march_blocks_per_sm = in->march_blocks_per_sm;
   b->shape.shade_blocks_per_sm = in->shade_blocks_per_sm;
+  b->shape.bil_rows = in->bilateral_rows ? in->bilateral_rows : 8;
+  b->shape.integrate_blocks_per_sm = in->integrate_blocks_per_sm;
   drop_graphs(b);  // recaptured with the new grids at the next step
   return VS_OK;
 }
 
-// Times the ray-cast stage of these sessions under every candidate launch
-// shape and keeps the fastest.  The ray-cast reads the volume and pose and
-// rewrites the model maps with the values the last step gave them (results
-// do not depend on the shape), so no session changes state.
+// Times three stages of these sessions under their candidate launch shapes
+// and keeps the fastest of each: the ray-cast (ray tile, march and shading
+// grids), the filter (rows of the bilateral / activation tile) and the
+// integration (update grid).  None of the shapes changes a result, and none
+// of the timing runs changes a session's state: the ray-cast and the filter
+// rewrite their outputs with the values the last step gave them, and the
+// integration runs as a dry run (every voxel computed, none stored; its
+// activation lists the same sub-cubes again).
+namespace {
+
+int time_launches(cudaStream_t st, int reps, cudaEvent_t e0, cudaEvent_t e1, const std::function<void()>& f,
+                  float* ms) {
+  cudaError_t e = cudaSuccess;
+  for (int r = 0; r <= reps && e == cudaSuccess; r++) {
+    if (r == 1) e = cudaEventRecord(e0, st);
+    f();
+    if (e == cudaSuccess) e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+  if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+  if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+  *ms /= (float)reps;
+  return e == cudaSuccess ? VS_OK : cuda_fail_code(e, "vs_batch_autotune");
+}
+
+}  // namespace
+
 int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps, vs_launch_shape* best,
                       float* best_ms) {
   if (!b || !sessions) return fail_code(VS_ERR_ARG, "null argument");
@@ -495,46 +527,73 @@ int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps,
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   cudaError_t e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_autotune");
   LaunchShape win = b->shape;
   float win_ms = 1e30f;
   BatchTable* t = b->h_tab[0];
-  for (int lx = 1; lx <= 5 && e == cudaSuccess; lx++) {
-    fill_batch_table(*t, hr, dr, n, lx);
-    e = cudaMemcpyAsync(b->d_tab, t, sizeof(BatchTable), cudaMemcpyHostToDevice, b->stream);
+  auto upload = [&](int lx, int rows) {
+    fill_batch_table(*t, hr, dr, n, lx, rows);
+    return cudaMemcpyAsync(b->d_tab, t, sizeof(BatchTable), cudaMemcpyHostToDevice, b->stream);
+  };
+  // ray-cast: ray tile and march grid
+  for (int lx = 1; lx <= 5 && rc == VS_OK; lx++) {
+    if (upload(lx, win.bil_rows) != cudaSuccess) rc = cuda_fail_code(cudaGetLastError(), "vs_batch_autotune");
     const int mcands[3] = {most_m, (most_m * 3) / 4, most_m / 2};
-    for (int c = 0; c < 3 && e == cudaSuccess; c++) {
+    for (int c = 0; c < 3 && rc == VS_OK; c++) {
       if (mcands[c] < 1 || (c > 0 && mcands[c] == mcands[c - 1])) continue;
-      LaunchShape sh;
+      LaunchShape sh = win;
       sh.ray_lx = lx;
       sh.march_blocks_per_sm = mcands[c];
       sh.shade_blocks_per_sm = most_s;
-      // one untimed launch, then reps timed ones
-      for (int r = 0; r <= reps && e == cudaSuccess; r++) {
-        if (r == 1) e = cudaEventRecord(e0, b->stream);
+      float ms = 0.0f;
+      rc = time_launches(b->stream, reps, e0, e1, [&] {
         launch_raycast(b->d_tab, k.tsdf_type, -1, nullptr, nullptr, nullptr, 0.0f, 0.0f, -1.0f, true, nullptr,
                        nullptr, nullptr, nullptr, b->stream, sh, nullptr, k.color != 0);
-        if (e == cudaSuccess) e = cudaGetLastError();
-      }
-      if (e == cudaSuccess) e = cudaEventRecord(e1, b->stream);
-      if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-      float ms = 0.0f;
-      if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-      ms /= (float)reps;
-      if (e == cudaSuccess && ms < win_ms) {
+      }, &ms);
+      if (rc == VS_OK && ms < win_ms) {
         win_ms = ms;
         win = sh;
       }
     }
   }
-  if (e0) cudaEventDestroy(e0);
-  if (e1) cudaEventDestroy(e1);
-  if (e != cudaSuccess) return cuda_fail_code(e, "vs_batch_autotune");
+  // filter: rows of the bilateral (and activation) tile
+  float fil_ms = 1e30f;
+  const int rows_c[3] = {8, 4, 16};
+  for (int c = 0; c < 3 && rc == VS_OK; c++) {
+    if (upload(win.ray_lx, rows_c[c]) != cudaSuccess) rc = cuda_fail_code(cudaGetLastError(), "vs_batch_autotune");
+    float ms = 0.0f;
+    if (rc == VS_OK) rc = time_launches(b->stream, reps, e0, e1, [&] { launch_filter(b->d_tab, b->stream, rows_c[c]); }, &ms);
+    if (rc == VS_OK && ms < fil_ms) {
+      fil_ms = ms;
+      win.bil_rows = rows_c[c];
+    }
+  }
+  // integration: update grid, as dry runs
+  if (rc == VS_OK && upload(win.ray_lx, win.bil_rows) != cudaSuccess)
+    rc = cuda_fail_code(cudaGetLastError(), "vs_batch_autotune");
+  float int_ms = 1e30f;
+  const int ib_c[3] = {0, 3, 2};
+  for (int c = 0; c < 3 && rc == VS_OK; c++) {
+    float ms = 0.0f;
+    rc = time_launches(b->stream, reps, e0, e1, [&] {
+      launch_integrate(b->d_tab, k.tsdf_type, nullptr, nullptr, nullptr, true, b->stream, k.color != 0, ib_c[c], true);
+    }, &ms);
+    if (rc == VS_OK && ms < int_ms) {
+      int_ms = ms;
+      win.integrate_blocks_per_sm = ib_c[c];
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) return rc;
   b->shape = win;
   drop_graphs(b);
   if (best) {
     best->ray_tile_log2 = win.ray_lx;
     best->march_blocks_per_sm = win.march_blocks_per_sm;
     best->shade_blocks_per_sm = win.shade_blocks_per_sm;
+    best->bilateral_rows = win.bil_rows;
+    best->integrate_blocks_per_sm = win.integrate_blocks_per_sm;
   }
   if (best_ms) *best_ms = win_ms;
   return VS_OK;

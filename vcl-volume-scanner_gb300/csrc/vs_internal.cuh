@@ -113,8 +113,9 @@ struct SessionDev {
 struct BatchTable {
   int n;
   int ray_lx;                          // ray tile of a warp: (1 << ray_lx) x (32 >> ray_lx) rays
+  int bil_rows;                        // rows of a level-0 tile (bilateral, activation): 4, 8 or 16
   const SessionDev* s[kMaxSlots];
-  int bil[kMaxSlots + 1];              // level-0 32x8 tiles (bilateral, activation)
+  int bil[kMaxSlots + 1];              // level-0 32 x bil_rows tiles (bilateral, activation)
   int pyr[kMaxLevels - 1][kMaxSlots + 1];  // 32x8 tiles of levels 1, 2
   int ipre[kMaxSlots + 1];             // input-map pre-pass 32x8 tiles, all levels
   int ipost[kMaxSlots + 1];            // input-map post-pass 16x16 tiles, all levels
@@ -287,14 +288,16 @@ struct LaunchShape {
   int ray_lx = 3;               // ray tile of a warp: (1 << ray_lx) x (32 >> ray_lx), ray_lx in 0..5
   int march_blocks_per_sm = 0;  // resident 128-thread blocks per SM of the march grid (0: as many as fit)
   int shade_blocks_per_sm = 0;
+  int bil_rows = 8;             // level-0 tile rows of the bilateral filter and the activation: 4, 8, 16
+  int integrate_blocks_per_sm = 0;  // 256-thread blocks per SM of the update grid (0: as many as fit)
 };
 
 int icp_blocks(int npix, int level);
 int sm_count();
 void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const SessionDev* const* dev_recs, int n,
-                      int ray_lx = 3);
+                      int ray_lx = 3, int bil_rows = 8);
 int ray_max_blocks_per_sm(int tsdf_type, bool shade);
-void launch_filter(const BatchTable* bt, cudaStream_t st);
+void launch_filter(const BatchTable* bt, cudaStream_t st, int bil_rows = 8);
 void launch_input_maps(const BatchTable* bt, cudaStream_t st);
 void launch_bilateral_float(const SessionDev& h, const float* in, float* out, cudaStream_t st);
 // ICP of every slot; the schedule runs levels max_levels-1 .. 0 with
@@ -304,8 +307,11 @@ void launch_icp(const BatchTable* bt, int max_levels, const int* max_iters, int 
 // depth / Tgc / Tcg: explicit inputs of a one-slot table, or NULL for each
 // session's own level-0 depth and pose; color: run the variant that also
 // blends the colour of sessions that keep a colour volume
+// blocks_per_sm: update grid (0: every block resident); dry: the update
+// computes everything but stores no voxel (the autotuner's timing runs)
 void launch_integrate(const BatchTable* bt, int tsdf_type, const float* depth, const float* Tgc,
-                      const float* Tcg, bool gate_on_tracking, cudaStream_t st, bool color = false);
+                      const float* Tcg, bool gate_on_tracking, cudaStream_t st, bool color = false,
+                      int blocks_per_sm = 0, bool dry = false);
 // level < 0: every level of every slot into the sessions' model maps; else
 // one level of a one-slot table into the external outputs with explicit poses;
 // color: the shading variant that also interpolates colour

@@ -110,7 +110,8 @@ VS_SESSION_WAITING, VS_SESSION_RESIDENT, VS_SESSION_CLOSED = 0, 1, 2
 
 class LaunchShape(ctypes.Structure):
     _fields_ = [("ray_tile_log2", ctypes.c_int), ("march_blocks_per_sm", ctypes.c_int),
-                ("shade_blocks_per_sm", ctypes.c_int)]
+                ("shade_blocks_per_sm", ctypes.c_int), ("bilateral_rows", ctypes.c_int),
+                ("integrate_blocks_per_sm", ctypes.c_int)]
 
 
 _P = ctypes.c_void_p
@@ -609,19 +610,24 @@ class Batch:
     def launch_shape(self):
         sh = LaunchShape()
         _check(self.lib.vs_batch_get_launch_shape(self.h, ctypes.byref(sh)))
-        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm)
+        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm, sh.bilateral_rows,
+                sh.integrate_blocks_per_sm)
 
-    def set_launch_shape(self, ray_tile_log2, march_blocks_per_sm=0, shade_blocks_per_sm=0):
-        sh = LaunchShape(ray_tile_log2, march_blocks_per_sm, shade_blocks_per_sm)
+    def set_launch_shape(self, ray_tile_log2, march_blocks_per_sm=0, shade_blocks_per_sm=0, bilateral_rows=0,
+                         integrate_blocks_per_sm=0):
+        sh = LaunchShape(ray_tile_log2, march_blocks_per_sm, shade_blocks_per_sm, bilateral_rows,
+                         integrate_blocks_per_sm)
         _check(self.lib.vs_batch_set_launch_shape(self.h, ctypes.byref(sh)))
 
     def autotune(self, sessions, reps=3):
-        """picks the fastest ray-cast launch shape for these sessions; returns (shape, ms)"""
+        """picks the fastest launch shape of the ray-cast, filter and integration
+        for these sessions; returns (shape, ray-cast ms)"""
         sh = LaunchShape()
         ms = ctypes.c_float(0.0)
         _check(self.lib.vs_batch_autotune(self.h, self._handles(sessions), len(sessions), reps, ctypes.byref(sh),
                                           ctypes.byref(ms)))
-        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm), ms.value
+        return (sh.ray_tile_log2, sh.march_blocks_per_sm, sh.shade_blocks_per_sm, sh.bilateral_rows,
+                sh.integrate_blocks_per_sm), ms.value
 
 
 class _Borrowed(Session):
