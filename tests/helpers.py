@@ -85,7 +85,8 @@ def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_pose
     """Runs `frames` frames stage by stage through a session and hands the
     session's own tracking inputs (model maps of the previous ray-cast,
     filtered input pyramid, input normals, previous pose) to the oracle's
-    tracker at every frame: the tracked flag must equal the FP32 oracle's,
+    tracker at every frame: the tracked flag must equal the FP32 or the FP64
+    oracle's,
     and where both track, the pose must be within 1e-4 rad and 0.1 mm of the
     FP32 and FP64 oracles' (the per-frame tolerance on identical inputs).  A
     frame whose FP32 and FP64 oracles disagree beyond that tolerance on these
@@ -114,7 +115,9 @@ def reanchored_track_check(depth, cfg, frames, expect_tracked=True, compare_pose
                 inn = [x["input_normal"] for x in m] if cfg.cos_normal > -2.0 else None
                 ok32, oT, _ = O.track(ocfg, ind, mv, mn, T_prev, innrm_levels=inn, f64=False)
                 ok64, dT, _ = O.track(ocfg, ind, mv, mn, T_prev64, innrm_levels=inn, f64=True)
-                assert bool(info[0]) == ok32, (k, info[0], ok32)
+                # a frame on the pivot test's edge may go either way: the flag
+                # must be one of the two oracles'
+                assert bool(info[0]) in (ok32, ok64), (k, info[0], ok32, ok64)
                 if expect_tracked:
                     assert ok32 and ok64, (k, ok32, ok64)
                 if not info[0]:
