@@ -266,6 +266,13 @@ int vs_set_pose(vs_session* s, const double* T_gc_f64);
  * count and the sum of b^2, as summed (FP64); x6 = the increment solved from
  * them (twist [w; v], rounded to float).  Either pointer may be NULL. */
 int vs_get_icp_system(vs_session* s, double* sums29, float* x6);
+/* Diagnostic of the ray-cast's free-space skipping (no reference
+ * counterpart): per sub-cube, x fastest (z * nb_x * nb_y + y * nb_x + x, nb =
+ * dim / 8), band = 1 where some voxel has weight > 0 and a TSDF value other
+ * than 1 (the only sub-cubes whose samples can change the march), and dist =
+ * the Chebyshev distance in sub-cubes to the nearest band sub-cube as the
+ * last ray-cast computed it, saturating at 8.  Either pointer may be NULL. */
+int vs_get_band(vs_session* s, uint8_t* band, uint8_t* dist);
 /* GKvObjectCube::to_host / from_host (_yooji_cuda_object_cube.hpp:6-85): the
  * volume in the reference's x-fastest layout (z*W*H + y*W + x), TSDF as float
  * and weight as uint16; either pointer may be NULL. */

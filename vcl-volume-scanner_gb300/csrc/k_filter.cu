@@ -430,6 +430,8 @@ void fill_batch_table(BatchTable& hb, const SessionDev* const* host_recs, const 
     for (int l = 0; l < kMaxLevels; l++)
       hb.icp[l][i + 1] = hb.icp[l][i] + (l < h.levels ? icp_blocks(h.lv[l].W * h.lv[l].H, l) : 0);
     hb.ray[i + 1] = hb.ray[i] + ray;
+    hb.slab[i + 1] = hb.slab[i] + (h.bdist ? h.nb[2] : 0);
+    hb.brow[i + 1] = hb.brow[i] + (h.bdist ? h.nb[1] : 0);
   }
 }
 

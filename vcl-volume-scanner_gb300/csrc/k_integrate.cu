@@ -145,9 +145,6 @@ struct IntParams {
   const float* lam_map;
   const uint32_t* list;
   uint32_t* counters;
-  uint32_t* occ;
-  uint32_t* occ1;
-  uint32_t* occ2;
   void* vol;
   uint32_t* col;            // colour bricks (NULL: no colour)
   const uint32_t* rgb;      // packed colour frame
@@ -156,7 +153,6 @@ struct IntParams {
   float K[4];
   float mu, max_w;
   int W, H, nb0, nb1, d0, d1;
-  int nc1[2], nc2[2];
 };
 
 __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ s, const float* depth_ext,
@@ -167,13 +163,6 @@ __device__ inline void load_params(IntParams& q, const SessionDev* __restrict__ 
   q.lam_map = s->lam_map;
   q.list = s->brick_list;
   q.counters = s->brick_count;
-  q.occ = s->occ;
-  q.occ1 = s->occ1;
-  q.occ2 = s->occ2;
-  q.nc1[0] = s->nc1[0];
-  q.nc1[1] = s->nc1[1];
-  q.nc2[0] = s->nc2[0];
-  q.nc2[1] = s->nc2[1];
   q.vol = s->vol;
   q.col = s->col;
   q.rgb = s->rgb_packed;
@@ -456,6 +445,7 @@ __global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
     }
     const uint32_t b = reload(sp->brick_list + (i - pre[lo]));
     int nupd = 0;
+    bool band = false;  // some voxel of the brick, after the update, is a band voxel
     const uint32_t nb0 = (uint32_t)reload(&sp->nb[0]), nb1 = (uint32_t)reload(&sp->nb[1]);
     const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / (nb0 * nb1));
     uint4* bv = reinterpret_cast<uint4*>(reinterpret_cast<word*>(reload(&sp->vol)) + (size_t)b * kBrickVox);
@@ -576,6 +566,10 @@ __global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
         color_round<S, kPerVec, kRound>(q, upd, r * kRound, lane, bx, by, bz, b, wv, lx, ly, lz);
 #pragma unroll
       for (int v = 0; v < kRV; v++)
+#pragma unroll
+        for (int e = 0; e < kPerVec; e++) band |= S::band(wv[v][e]);
+#pragma unroll
+      for (int v = 0; v < kRV; v++)
         if (changed[v] && !dry) {
           memcpy(&cur[v], wv[v], 16);
           bv[(r * kRV + v) * 32 + lane] = cur[v];
@@ -587,19 +581,17 @@ __global__ void __launch_bounds__(kIntThreads, COLOR ? 2 : VS_INT_MIN_BLOCKS)
     }
 #pragma unroll
     for (int m = 16; m >= 1; m >>= 1) nupd += __shfl_xor_sync(0xffffffffu, nupd, m);
-    if (lane == 0) {
+    band = __any_sync(0xffffffffu, band);
+    if (lane == 0 && !dry) {
+      // the brick's band state from its words after this update (the
+      // brick's own warp is its only writer)
+      uint8_t* bb = reload(&sp->band);
+      if (bb) bb[b] = band ? 1 : 0;
       if (nupd) {
         atomicAdd(reload(&sp->brick_count) + 1, (uint32_t)nupd);
-        // weights never decrease, so a brick that got an update, and the
-        // occupancy cells around it, stay occupied
+        // weights never decrease, so a brick that got an update stays occupied
         uint32_t* occ = reload(&sp->occ);
-        if (occ) {
-          const int nc1[2] = {reload(&sp->nc1[0]), reload(&sp->nc1[1])};
-          const int nc2[2] = {reload(&sp->nc2[0]), reload(&sp->nc2[1])};
-          set_bit_once(occ, b);
-          set_bit_once(reload(&sp->occ1), occ_cell(bx, by, bz, kOcc1Shift, nc1));
-          set_bit_once(reload(&sp->occ2), occ_cell(bx, by, bz, kOcc2Shift, nc2));
-        }
+        if (occ) set_bit_once(occ, b);
       }
     }
   }
@@ -645,7 +637,7 @@ __global__ void k_volume_import(typename S::word* vol, int X, int Y, int z0, int
   }
 }
 
-// recomputes the occupancy bits from the weights (after a volume import);
+// recomputes the occupancy bits and band flags from the volume (after an import);
 // one warp per brick
 template <class S>
 __global__ void k_occupancy(const SessionDev* __restrict__ s) {
@@ -656,19 +648,20 @@ __global__ void k_occupancy(const SessionDev* __restrict__ s) {
   const size_t gw = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const size_t nwarp = ((size_t)gridDim.x * blockDim.x) >> 5;
   for (size_t b = gw; b < nbr; b += nwarp) {
-    bool any = false;
+    bool any = false, band = false;
     for (int k = lane; k < kBrickVox; k += 32) {
+      const typename S::word v = vol[b * kBrickVox + k];
       float t;
       uint32_t w;
-      S::decode(vol[b * kBrickVox + k], t, w);
+      S::decode(v, t, w);
       any |= w != 0u;
+      band |= S::band(v);
     }
     const unsigned m = __ballot_sync(0xffffffffu, any);
-    if (lane == 0 && m) {
-      const int bx = (int)(b % nb0), by = (int)((b / nb0) % nb1), bz = (int)(b / ((size_t)nb0 * nb1));
-      set_bit_once(s->occ, (uint32_t)b);
-      set_bit_once(s->occ1, occ_cell(bx, by, bz, kOcc1Shift, s->nc1));
-      set_bit_once(s->occ2, occ_cell(bx, by, bz, kOcc2Shift, s->nc2));
+    band = __any_sync(0xffffffffu, band);
+    if (lane == 0) {
+      if (m) set_bit_once(s->occ, (uint32_t)b);
+      if (s->band) s->band[b] = band ? 1 : 0;
     }
   }
 }
@@ -867,22 +860,18 @@ __global__ void k_carve(const SessionDev* __restrict__ s, const uint8_t* __restr
       for (int k = lane; k < kBrickVox; k += 32) s->col[b * kBrickVox + k] = 0u;
     if (lane == 0) {
       s->brick_flag[b] = 0u;
+      if (s->band) s->band[b] = 0;
       atomicAnd(s->occ + (b >> 5), ~(1u << (b & 31)));
       atomicAdd(carved, 1u);
     }
   }
 }
 
-size_t occupancy_words(const SessionDev& h, int level) {
-  if (level == 0) return (((size_t)h.nb[0] * h.nb[1] * h.nb[2]) + 31) / 32;
-  const int* nc = level == 1 ? h.nc1 : h.nc2;
-  return (((size_t)nc[0] * nc[1] * nc[2]) + 31) / 32;
-}
+size_t occupancy_words(const SessionDev& h) { return (((size_t)h.nb[0] * h.nb[1] * h.nb[2]) + 31) / 32; }
 
 void launch_occupancy_clear(const SessionDev& h, cudaStream_t st) {
-  cudaMemsetAsync(h.occ, 0, occupancy_words(h, 0) * 4, st);
-  cudaMemsetAsync(h.occ1, 0, occupancy_words(h, 1) * 4, st);
-  cudaMemsetAsync(h.occ2, 0, occupancy_words(h, 2) * 4, st);
+  cudaMemsetAsync(h.occ, 0, occupancy_words(h) * 4, st);
+  if (h.band) cudaMemsetAsync(h.band, 0, (size_t)h.nb[0] * h.nb[1] * h.nb[2], st);
 }
 
 void launch_occupancy_rebuild(const SessionDev& h, const SessionDev* d, cudaStream_t st) {

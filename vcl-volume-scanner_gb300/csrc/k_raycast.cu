@@ -48,16 +48,15 @@ struct RayArgs {
 
 // Volume reads.  A brick whose occupancy bit is clear has weight 0 in every
 // voxel (weights only grow), so its voxels answer "no value" from a 32 KB
-// bitmap that stays in L1 instead of a volume gather: free-space steps of the
-// march cost no HBM traffic, with results identical to reading the voxel.
+// bitmap that stays in L1 instead of a volume gather, with results identical
+// to reading the voxel.
 template <class S>
 struct Vol {
   const typename S::word* v;
   const uint32_t* occ;
-  const uint32_t* occ1;  // cells of 2^kOcc1Shift bricks per axis
-  const uint32_t* occ2;  // cells of 2^kOcc2Shift bricks per axis
+  const uint8_t* bdist;  // distance in bricks to the nearest band brick
   int dim[3];
-  int nc1[3], nc2[3];
+  uint32_t nbx, nbxy;  // bricks per row / per slab
   uint32_t sy, sz;  // word strides of one brick row / one brick slab: 512 nb[0], 512 nb[0] nb[1]
   // The word index of voxel (x, y, z) >= 0 is the sum of one term per axis
   // (brick part + offset inside the brick), in 32 bits (volumes of at most
@@ -73,67 +72,85 @@ struct Vol {
     S::decode(__ldg(v + i), t, w);
     return w != 0u;
   }
-  __device__ inline bool cell_set(const uint32_t* bits, const int* nc, int shift, int x, int y, int z) const {
-    const uint32_t c = ((uint32_t)(z >> shift) * (uint32_t)nc[1] + (uint32_t)(y >> shift)) * (uint32_t)nc[0] +
-                       (uint32_t)(x >> shift);
-    return (__ldg(bits + (c >> 5)) >> (c & 31)) & 1u;
-  }
   // Free-space run: how many of the next steps p + k inc (k = 1..m) are
-  // certain to read "no value" - outside the volume, or inside an empty
-  // occupancy cell - so that the march only has to advance the position for
-  // them.  The bounds are pulled in by 0.05 voxel, far more than the
-  // rounding of the position accumulated over a run (at most 64 steps of
-  // float additions, under 1e-2 voxel for coordinates below 2048) or of the
-  // approximate reciprocals of the increment.  A negative result -k says the
-  // position lies in an occupied occ1 cell that the ray leaves after about k
-  // steps; the caller need not ask again before then (asking late only
-  // delays a run, it never changes a sample).
-  // A NaN coordinate fails every comparison below and gives 0.
+  // certain to read TSDF 1 ("no value", or a voxel whose value is 1) -
+  // outside the volume, or inside the box of bricks that holds no band brick
+  // (the bricks within Chebyshev distance bdist - 1 of a position's brick) -
+  // so that the march only has to advance the position for them.  Boxes are
+  // chained: the step after a box joins the run when it certainly reads 1
+  // too, and the next box starts there.  The bounds are pulled in by 0.05
+  // voxel, far more than the rounding of a position p + k inc (one product
+  // and one sum: under 1e-3 voxel for k <= kMaxRun and coordinates below
+  // 2048) or of the approximate reciprocals of the increment, so a step
+  // counted here reads 1 however its position rounds.  A negative result -k
+  // says p lies in a band brick that the ray leaves after about k steps; the
+  // caller need not ask again before then (asking late only delays a run, it
+  // never changes a sample).  A NaN coordinate fails every comparison below
+  // and gives 0.
+  static constexpr int kMaxRun = 4096;
+  static constexpr int kMaxBoxes = 3;
   __device__ inline int free_run(F3 p, F3 inc) const {
     const float d = 0.05f;
     const float pa[3] = {p.x, p.y, p.z}, ia[3] = {inc.x, inc.y, inc.z};
     const float ra[3] = {__fdividef(1.0f, inc.x), __fdividef(1.0f, inc.y), __fdividef(1.0f, inc.z)};
-    // a coordinate is in range iff -0.5 < p < dim - 0.5 (gtvu rounds with ROUNDF)
-    bool inside = true;
+    int run = 0;
+    for (int j = 0; j < kMaxBoxes; j++) {
+      // q: step `run` (j = 0: the current sample, which read 1; after that
+      // the step following the last box, a candidate for the run)
+      float q[3];
 #pragma unroll
-    for (int a = 0; a < 3; a++) inside &= pa[a] > -0.5f && pa[a] < (float)dim[a] - 0.5f;
-    float t;
-    bool occupied_cell = false;
-    if (!inside) {
-      // outside until every coordinate that is out of range has come in
-      t = 0.0f;
+      for (int a = 0; a < 3; a++) q[a] = j == 0 ? pa[a] : (float)run * ia[a] + pa[a];
+      // a coordinate is in range iff -0.5 < q < dim - 0.5 (gtvu rounds with ROUNDF)
+      bool inside = true;
 #pragma unroll
-      for (int a = 0; a < 3; a++) {
-        const float hi = (float)dim[a] - 0.5f;
-        if (pa[a] <= -0.5f)
-          t = fmaxf(t, ia[a] > 0.0f ? (-0.5f - d - pa[a]) * ra[a] : 1e30f);
-        else if (pa[a] >= hi)
-          t = fmaxf(t, ia[a] < 0.0f ? (hi + d - pa[a]) * ra[a] : 1e30f);
+      for (int a = 0; a < 3; a++) inside &= q[a] > -0.5f && q[a] < (float)dim[a] - 0.5f;
+      float t;
+      bool band = false, sure = false;  // sure: q reads 1 however it rounds
+      if (!inside) {
+        // outside until every coordinate that is out of range has come in
+        t = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          const float hi = (float)dim[a] - 0.5f;
+          if (q[a] <= -0.5f) {
+            t = fmaxf(t, ia[a] > 0.0f ? (-0.5f - d - q[a]) * ra[a] : 1e30f);
+            sure |= q[a] < -0.5f - d;
+          } else if (q[a] >= hi) {
+            t = fmaxf(t, ia[a] < 0.0f ? (hi + d - q[a]) * ra[a] : 1e30f);
+            sure |= q[a] > hi + d;
+          }
+        }
+      } else {
+        // inside: every coordinate > -0.5, where ROUNDF is (int)(q + 0.5);
+        // brick b holds the nearest voxel, and the box of bricks b - h ..
+        // b + h (h = bdist - 1) holds no band brick; in a band brick (bdist
+        // 0) the box is the brick itself
+        const int b[3] = {(int)(q[0] + 0.5f) >> 3, (int)(q[1] + 0.5f) >> 3, (int)(q[2] + 0.5f) >> 3};
+        const int dist = __ldg(bdist + (uint32_t)b[2] * nbxy + (uint32_t)b[1] * nbx + (uint32_t)b[0]);
+        band = dist == 0;
+        sure = !band;
+        const int h = band ? 0 : dist - 1;
+        t = 1e30f;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+          const float lo = (float)((b[a] - h) * 8) - 0.5f, hi = (float)((b[a] + h + 1) * 8) - 0.5f;
+          sure &= q[a] > lo + d && q[a] < hi - d;
+          if (ia[a] > 0.0f)
+            t = fminf(t, (hi - d - q[a]) * ra[a]);
+          else if (ia[a] < 0.0f)
+            t = fminf(t, (lo + d - q[a]) * ra[a]);
+        }
       }
-    } else {
-      // inside: every coordinate > -0.5, where ROUNDF is (int)(p + 0.5)
-      const int x = (int)(p.x + 0.5f), y = (int)(p.y + 0.5f), z = (int)(p.z + 0.5f);
-      int size = 8 << kOcc1Shift;
-      if (!cell_set(occ2, nc2, kOcc2Shift + 3, x, y, z))
-        size = 8 << kOcc2Shift;
-      else if (cell_set(occ1, nc1, kOcc1Shift + 3, x, y, z))
-        occupied_cell = true;
-      const int c[3] = {x & ~(size - 1), y & ~(size - 1), z & ~(size - 1)};
-      t = 1e30f;
-#pragma unroll
-      for (int a = 0; a < 3; a++) {
-        const float lo = (float)c[a] - 0.5f, hi = lo + (float)size;
-        if (ia[a] > 0.0f)
-          t = fminf(t, (hi - d - pa[a]) * ra[a]);
-        else if (ia[a] < 0.0f)
-          t = fminf(t, (lo + d - pa[a]) * ra[a]);
-      }
+      if (j > 0 && !sure) return run - 1;
+      // steps k >= 1 from q with k < t
+      t = fminf(t, (float)(kMaxRun + 1));
+      const int m = (int)ceilf(t) - 1;
+      if (j == 0 && band) return m > 0 ? -m : 0;
+      run += m > 0 ? m : 0;
+      if (run >= kMaxRun) return run;
+      run++;  // the next candidate
     }
-    // steps k >= 1 with k < t
-    t = fminf(t, 65.0f);
-    const int m = (int)ceilf(t) - 1;
-    if (occupied_cell) return m > 0 ? -m : 0;
-    return m > 0 ? m : 0;
+    return run - 1;
   }
 
   // d_gtvu_Get_TSDF_Value_Uninterpolated: nearest voxel (ROUNDF), weight > 0.
@@ -314,14 +331,15 @@ __device__ bool cast_ray(const Vol<S>& V, const SessionDev& s, const float* K, f
       }
     }
     if (tsdf == 1.0f && state != BEHIND && --recheck < 0) {
-      // While samples read "no value" (TSDF 1) the state and the step stay as
-      // they are, so the `run` steps of a free-space run are taken at once:
-      // p + run * inc and total + run * sn.  The step-by-step sums of the
-      // reference round after every step; the jump rounds once, so the
-      // position after a run differs from theirs by at most a few ulps of the
-      // voxel coordinate (under 1e-3 voxel for coordinates below 1024), which
-      // moves the later samples and the surface point by far less than the
-      // 1 mm ray-cast tolerance.
+      // While samples read TSDF 1 (no value, or a voxel whose value is 1) the
+      // state and the step stay as they are, so the `run` steps of a
+      // free-space run are taken at once: p + run * inc and total + run * sn.
+      // The step-by-step sums of the reference round after every step; the
+      // jump rounds once, so the position after a run of m steps differs
+      // from theirs by at most about m / 2 ulps of the voxel coordinate
+      // (under 1e-2 voxel for runs of a few hundred steps and coordinates
+      // below 1024), which moves the later samples and the surface point by
+      // far less than the 1 mm ray-cast tolerance.
       const float sn = (state == COARSE) ? step_scale : fmaxf(step_scale * tsdf, 1.0f);
       const F3 inc = scale(sn, rd);
       int m = V.free_run(vs, inc);
@@ -420,12 +438,91 @@ __device__ inline Vol<S> volume_of(const SessionDev& s) {
   Vol<S> V;
   V.v = reinterpret_cast<const typename S::word*>(s.vol);
   V.occ = s.occ;
-  V.occ1 = s.occ1;
-  V.occ2 = s.occ2;
-  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k], V.nc1[k] = s.nc1[k], V.nc2[k] = s.nc2[k];
+  V.bdist = s.bdist;
+  for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k];
+  V.nbx = (uint32_t)s.nb[0];
+  V.nbxy = (uint32_t)s.nb[0] * (uint32_t)s.nb[1];
   V.sy = (uint32_t)s.nb[0] << 9;
   V.sz = ((uint32_t)s.nb[0] * (uint32_t)s.nb[1]) << 9;
   return V;
+}
+
+// Band distance field (the Chebyshev distance transform of the band bricks,
+// saturating at kBandReach + 1), separable: the distance along x to the
+// nearest band brick of the row, then per brick the minimum over its column
+// of max(|dy|, x distance), then the same along z.  Each pass holds one plane
+// of bricks in shared memory and evaluates its 2 kBandReach + 1 window
+// without data-dependent exits, so the reads of a brick's window are
+// independent.
+constexpr int kBandSat = kBandReach + 1;
+constexpr int kBandThreads = 1024;
+
+// d(i) = min over |k| <= kBandReach of max(|k|, in[i + k * stride]), for
+// positions inside [0, n) along the pass's axis (c: the brick's coordinate)
+__device__ inline int band_window(const uint8_t* in, int i, int c, int n, int stride) {
+  int d = in[i];
+#pragma unroll
+  for (int k = 1; k <= kBandReach; k++) {
+    const int lo = c - k >= 0 ? in[i - k * stride] : kBandSat;
+    const int hi = c + k < n ? in[i + k * stride] : kBandSat;
+    d = min(d, max(k, min(lo, hi)));
+  }
+  return d;
+}
+
+// i / n for 0 <= i < 2^14 and 1 <= n <= 128 without an integer division:
+// (i + 0.5) / n lies at least 0.5 / n from every integer, far more than the
+// float rounding of (i + 0.5) * (1 / n)
+__device__ inline int small_div(int i, float inv_n) { return (int)(((float)i + 0.5f) * inv_n); }
+
+// x and y passes, one block per z slab of a session: band flags (0 / 1) ->
+// x distances -> xy distances
+__global__ void __launch_bounds__(kBandThreads) k_band_xy(const BatchTable* __restrict__ bt) {
+  __shared__ uint8_t sb[kMaxBricksAxis * kMaxBricksAxis];
+  __shared__ uint8_t sx[kMaxBricksAxis * kMaxBricksAxis];
+  const int n = bt->n;
+  const int total = bt->slab[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int z;
+    const SessionDev* __restrict__ s = bt->s[find_slot(bt->slab, n, item, z)];
+    const int nb0 = s->nb[0], nb1 = s->nb[1], np = nb0 * nb1;
+    const float inv0 = 1.0f / (float)nb0;
+    const uint8_t* __restrict__ band = s->band + (size_t)z * np;
+    __syncthreads();  // the previous slab's reads of sb / sx are done
+    // a band brick is at distance 0, any other at "not yet found"
+    for (int i = threadIdx.x; i < np; i += blockDim.x) sb[i] = band[i] ? 0 : kBandSat;
+    __syncthreads();
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+      sx[i] = (uint8_t)band_window(sb, i, i - small_div(i, inv0) * nb0, nb0, 1);
+    __syncthreads();
+    uint8_t* __restrict__ out = s->btmp + (size_t)z * np;
+    for (int i = threadIdx.x; i < np; i += blockDim.x) out[i] = (uint8_t)band_window(sx, i, small_div(i, inv0), nb1, nb0);
+  }
+}
+
+// z pass, one block per y row of a session: the x-z plane of xy distances in
+// shared memory -> distances
+__global__ void __launch_bounds__(kBandThreads) k_band_z(const BatchTable* __restrict__ bt) {
+  __shared__ uint8_t sp[kMaxBricksAxis * kMaxBricksAxis];
+  const int n = bt->n;
+  const int total = bt->brow[n];
+  for (int item = blockIdx.x; item < total; item += gridDim.x) {
+    int y;
+    const SessionDev* __restrict__ s = bt->s[find_slot(bt->brow, n, item, y)];
+    const int nb0 = s->nb[0], nb2 = s->nb[2], np = nb0 * s->nb[1], nq = nb0 * nb2;
+    const float inv0 = 1.0f / (float)nb0;
+    __syncthreads();  // the previous row's reads of sp are done
+    // plane element (x, z) at z * nb0 + x; brick z * np + y * nb0 + x
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+      const int z = small_div(i, inv0);
+      sp[i] = s->btmp[(size_t)z * (np - nb0) + (size_t)y * nb0 + i];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < nq; i += blockDim.x) {
+      const int z = small_div(i, inv0);
+      s->bdist[(size_t)z * (np - nb0) + (size_t)y * nb0 + i] = (uint8_t)band_window(sp, i, z, nb2, nb0);
+    }
+  }
 }
 
 #ifndef VS_RAY_MIN_BLOCKS
@@ -631,6 +728,8 @@ int grid_of(int want, int most) { return sm_count() * ((want > 0 && want < most)
 template <class S>
 void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, bool color, cudaStream_t st) {
   RayArgs a = a0;
+  k_band_xy<<<sm_count() * 2, kBandThreads, 0, st>>>(a.bt);
+  k_band_z<<<sm_count() * 2, kBandThreads, 0, st>>>(a.bt);
   if (a.mode & kRayScene)
     k_ray_march<S, true><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
   else

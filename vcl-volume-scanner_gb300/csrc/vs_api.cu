@@ -95,8 +95,6 @@ void fill_geometry(const vs_config* c, SessionDev& h) {
   for (int k = 0; k < 3; k++) {
     h.dim[k] = c->dim[k];
     h.nb[k] = c->dim[k] / 8;
-    h.nc1[k] = (h.nb[k] + (1 << kOcc1Shift) - 1) >> kOcc1Shift;
-    h.nc2[k] = (h.nb[k] + (1 << kOcc2Shift) - 1) >> kOcc2Shift;
     h.origin[k] = c->origin[k];
   }
   h.vox = c->voxel_size;
@@ -278,7 +276,7 @@ size_t vs_session_bytes(const vs_config* c) {
   if (check_config(c) != VS_OK) return 0;
   size_t b = volume_bytes(c);
   size_t nbr = (size_t)(c->dim[0] / 8) * (c->dim[1] / 8) * (c->dim[2] / 8);
-  b += 2 * nbr * 4 + 3 * (((nbr + 31) / 32) * 4) + 64;
+  b += 2 * nbr * 4 + ((nbr + 31) / 32) * 4 + 3 * nbr + 64;
   int w = c->width, h = c->height;
   b += (size_t)w * h * (2 + 4 + 4);
   for (int l = 0; l < c->levels; l++) {
@@ -329,9 +327,10 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
   rc |= alloc(s, &h.brick_flag, nbr * 4);
   rc |= alloc(s, &h.brick_list, nbr * 4);
   rc |= alloc(s, &h.brick_count, 64);
-  rc |= alloc(s, &h.occ, occupancy_words(h, 0) * 4);
-  rc |= alloc(s, &h.occ1, occupancy_words(h, 1) * 4);
-  rc |= alloc(s, &h.occ2, occupancy_words(h, 2) * 4);
+  rc |= alloc(s, &h.occ, occupancy_words(h) * 4);
+  rc |= alloc(s, &h.band, nbr);
+  rc |= alloc(s, &h.bdist, nbr);
+  rc |= alloc(s, &h.btmp, nbr);
   rc |= alloc(s, &h.depth_mm, n0 * 2);
   rc |= alloc(s, &h.depth_raw, n0 * 4);
   rc |= alloc(s, &s->stage_f, n0 * 4);
@@ -718,6 +717,15 @@ int vs_get_icp_system(vs_session* s, double* sums29, float* x6) {
   VS_CU(cudaStreamSynchronize(s->stream));
   if (sums29) std::memcpy(sums29, s->host_pose->last_sums, sizeof(s->host_pose->last_sums));
   if (x6) std::memcpy(x6, s->host_pose->last_x, sizeof(s->host_pose->last_x));
+  return VS_OK;
+}
+
+int vs_get_band(vs_session* s, uint8_t* band, uint8_t* dist) {
+  if (!s) return fail(VS_ERR_ARG, "null session");
+  const size_t nbr = (size_t)s->h.nb[0] * s->h.nb[1] * s->h.nb[2];
+  if (band) VS_CU(cudaMemcpyAsync(band, s->h.band, nbr, cudaMemcpyDeviceToHost, s->stream));
+  if (dist) VS_CU(cudaMemcpyAsync(dist, s->h.bdist, nbr, cudaMemcpyDeviceToHost, s->stream));
+  VS_CU(cudaStreamSynchronize(s->stream));
   return VS_OK;
 }
 

@@ -82,9 +82,11 @@ struct SessionDev {
   uint32_t* brick_list;          // active bricks of this frame
   uint32_t* brick_count;         // [0] active bricks, [1] voxels updated (per frame), [2] activation stamp
   uint32_t* occ;                 // 1 bit per brick: some voxel has weight > 0 (NULL: not kept)
-  uint32_t* occ1;                // 1 bit per occ1 cell (default 4^3 bricks): some brick occupied
-  uint32_t* occ2;                // 1 bit per 16^3 bricks (128^3 voxels)
-  int nc1[3], nc2[3];            // cells per axis of occ1 / occ2
+  uint8_t* band;                 // per brick: 1 if some voxel has weight > 0 and a TSDF value other
+                                 // than 1 (a superset is allowed; NULL: not kept)
+  uint8_t* bdist;                // per brick: Chebyshev distance in bricks to the nearest band brick,
+                                 // saturating at kBandReach + 1 (rebuilt before every ray-cast)
+  uint8_t* btmp;                 // the distance transform's intermediate (x and y passes)
   // ICP scratch
   double* partials;              // [kIcpMaxBlocks][2*kPartials]
   unsigned* icp_counter;
@@ -122,6 +124,8 @@ struct BatchTable {
   int scan[kMaxSlots + 1];             // input-map row scans: one per level
   int icp[kMaxLevels][kMaxSlots + 1];  // ICP block ranges per level
   int ray[kMaxSlots + 1];              // ray-cast tiles, all levels
+  int slab[kMaxSlots + 1];             // z slabs of bricks (band distance, x and y passes)
+  int brow[kMaxSlots + 1];             // y rows of bricks (band distance, z pass)
   unsigned work[8];                    // work counters ([0..1] ray march, [2..3] ICP, [4..5] ray
                                        // shading); zero between launches
 };
@@ -204,24 +208,17 @@ __device__ inline F3 pos_in_world(F3 v, const SessionDev& s) {
 __host__ __device__ inline uint32_t pack_rgb(uint32_t r, uint32_t g, uint32_t b) { return r | (g << 8) | (b << 16); }
 __host__ __device__ inline uint32_t rgb_channel(uint32_t w, int k) { return (w >> (8 * k)) & 0xffu; }
 
-// The two coarse occupancy levels: cells of 2^kOcc1Shift and 2^kOcc2Shift
-// bricks per axis (32^3 and 128^3 voxels by default).  Only the ray-cast's
-// free-space skipping reads them, so they change speed, never a result.
-#ifndef VS_OCC1_BRICK_SHIFT
-#define VS_OCC1_BRICK_SHIFT 2
-#endif
-#ifndef VS_OCC2_BRICK_SHIFT
-#define VS_OCC2_BRICK_SHIFT 4
-#endif
-constexpr int kOcc1Shift = VS_OCC1_BRICK_SHIFT;
-constexpr int kOcc2Shift = VS_OCC2_BRICK_SHIFT;
-
-// occupancy cell index of brick (bx, by, bz) at level `shift` (kOcc1Shift or
-// kOcc2Shift) in a grid of nc cells per axis
-__host__ __device__ inline uint32_t occ_cell(int bx, int by, int bz, int shift, const int* nc) {
-  return ((uint32_t)(bz >> shift) * (uint32_t)nc[1] + (uint32_t)(by >> shift)) * (uint32_t)nc[0] +
-         (uint32_t)(bx >> shift);
-}
+// Band bricks and their distance field.  A ray-cast sample reads TSDF 1
+// wherever the nearest voxel has weight 0 or value 1, and such samples leave
+// the march's state and step unchanged; only a "band" brick (a voxel with
+// weight > 0 and a value other than 1) can change them.  Before every ray-cast
+// the Chebyshev distance (in bricks) from every brick to the nearest band
+// brick is rebuilt, saturating at kBandReach + 1, so the march jumps through
+// the box of bricks around its position that holds no band brick.  The field
+// changes speed, never a sample.  Volumes have at most kMaxBricksAxis bricks
+// per axis (1024 voxels).
+constexpr int kBandReach = 7;
+constexpr int kMaxBricksAxis = 128;
 
 // sets bit i of a bitmap unless it is set already (the test keeps the atomics
 // off words whose bits all settled in earlier frames)
@@ -252,6 +249,8 @@ struct StoreI16 {
     return (w << 16) | ((uint32_t)(uint16_t)(int16_t)tsdf_to_q(t));
   }
   __device__ static inline word initial() { return (uint32_t)(uint16_t)(int16_t)32767; }
+  // weight > 0 and a value other than 1 (code 32767 is the only one that decodes to 1)
+  __device__ static inline bool band(word v) { return v >= 0x10000u && (v & 0xffffu) != 0x7fffu; }
 };
 struct StoreF16 {
   typedef uint32_t word;
@@ -263,6 +262,7 @@ struct StoreF16 {
     return (w << 16) | (uint32_t)__half_as_ushort(__float2half_rn(t));
   }
   __device__ static inline word initial() { return (uint32_t)__half_as_ushort(__float2half_rn(1.0f)); }
+  __device__ static inline bool band(word v) { return v >= 0x10000u && (v & 0xffffu) != 0x3c00u; }
 };
 struct StoreF32 {
   typedef uint2 word;
@@ -272,6 +272,7 @@ struct StoreF32 {
   }
   __device__ static inline word encode(float t, uint32_t w) { return make_uint2(__float_as_uint(t), w); }
   __device__ static inline word initial() { return make_uint2(__float_as_uint(1.0f), 0u); }
+  __device__ static inline bool band(word v) { return v.y != 0u && v.x != 0x3f800000u; }
 };
 
 inline size_t voxel_bytes(int tsdf_type) { return tsdf_type == VS_TSDF_FP32 ? 8 : 4; }
@@ -338,7 +339,7 @@ void launch_volume_init(const SessionDev& h, cudaStream_t st);
 void launch_pose_set(const SessionDev* d, const double* T_gc, cudaStream_t st);
 // pose heads of every slot, kPoseHeadBytes each, into out (kMaxSlots slots)
 void launch_gather_heads(const BatchTable* bt, void* out, cudaStream_t st);
-size_t occupancy_words(const SessionDev& h, int level);  // level 0: bricks, 1: 4^3, 2: 16^3 bricks
+size_t occupancy_words(const SessionDev& h);  // 32-bit words of the per-brick occupancy bits
 void launch_occupancy_clear(const SessionDev& h, cudaStream_t st);
 void launch_occupancy_rebuild(const SessionDev& h, const SessionDev* d, cudaStream_t st);
 void launch_maps_export(const SessionDev& h, int level, float* vtx3, float* nrm3, float* ivtx3, float* inrm3,

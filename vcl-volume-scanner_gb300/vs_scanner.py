@@ -141,6 +141,7 @@ _SIGS = {
     "vs_stage_raycast": (_I, [_P]),
     "vs_get_pose": (_I, [_P, _P, _P, _P]),
     "vs_get_icp_system": (_I, [_P, _P, _P]),
+    "vs_get_band": (_I, [_P, _P, _P]),
     "vs_set_pose": (_I, [_P, _P]),
     "vs_get_volume": (_I, [_P, _P, _P]),
     "vs_set_volume": (_I, [_P, _P, _P]),
@@ -476,6 +477,14 @@ class Session:
         x = np.empty(6, np.float32)
         _check(self.lib.vs_get_icp_system(self.h, _ptr(sums), _ptr(x)))
         return sums, x
+
+    def band(self):
+        """(band flags, band distances) per sub-cube, shaped (nb_z, nb_y, nb_x)"""
+        nb = [self.cfg.dim[k] // 8 for k in range(3)]
+        band = np.empty((nb[2], nb[1], nb[0]), np.uint8)
+        dist = np.empty((nb[2], nb[1], nb[0]), np.uint8)
+        _check(self.lib.vs_get_band(self.h, _ptr(band), _ptr(dist)))
+        return band, dist
 
     def set_pose(self, T_gc):
         Td = np.ascontiguousarray(T_gc, dtype=np.float64).reshape(16)
