@@ -241,6 +241,22 @@ def traffic_per_unit(kernel_key, unit_key):
     return None
 
 
+def raycast_per_unit(key):
+    """(per ray, per sub-cube) figure of the ray-cast stage's kernels from the
+    committed ncu summary: the march-and-shade kernel per ray, the two passes
+    of the band distance field per sub-cube; key "dram_bytes" or "warp_inst" """
+    r = traffic_per_unit("k_ray_fused", key + "_per_ray")
+    bx = traffic_per_unit("k_band_xy", key + "_per_brick")
+    bz = traffic_per_unit("k_band_z", key + "_per_brick")
+    if r is None or bx is None or bz is None:
+        return None
+    return r, bx + bz
+
+
+def level_bricks(cfg):
+    return (cfg.dim[0] // 8) * (cfg.dim[1] // 8) * (cfg.dim[2] // 8)
+
+
 def level_pixels(cfg):
     return [(cfg.width >> l) * (cfg.height >> l) for l in range(cfg.levels)]
 
@@ -692,17 +708,17 @@ def run_ours(args):
     dom_i = int(np.argmax(stage_sum))
     dom = names[dom_i]
     achieved = {k: alg[k] / (stage_sum[names.index(k)] * 1e-3) / 1e9 for k in names}
-    kernel_key = {"integrate": "k_integrate", "raycast": "k_ray_march+k_ray_shade", "track": "k_icp_iter",
+    kernel_key = {"integrate": "k_integrate", "raycast": "k_band_xy+k_band_z+k_ray_fused", "track": "k_icp_iter",
                   "filter": "k_bilateral_batch"}[dom]
     # measured DRAM bytes of one step of the stage: per-unit figures of the
     # committed ncu captures times this workload's units per step
     rays = np.mean([sum(sum(level_pixels(seqs[i]["cfg"])) for i in members[r]) for r in stage_steps])
+    bricks = np.mean([sum(level_bricks(seqs[i]["cfg"]) for i in members[r]) for r in stage_steps])
     traffic = None
     if dom == "raycast":
-        a_, b_ = traffic_per_unit("k_ray_march", "dram_bytes_per_ray"), traffic_per_unit("k_ray_shade",
-                                                                                          "dram_bytes_per_ray")
-        if a_ is not None and b_ is not None:
-            traffic = (a_ + b_) * rays
+        pu = raycast_per_unit("dram_bytes")
+        if pu is not None:
+            traffic = pu[0] * rays + pu[1] * bricks
     elif dom == "track":
         px = traffic_per_unit("k_icp_iter", "dram_bytes_per_pixel")
         if px is not None:
@@ -712,7 +728,7 @@ def run_ours(args):
                 "achieved": achieved[dom], "peak": peak, "unit": "GB/s", "frac": achieved[dom] / peak,
                 "traffic": traffic,
                 "traffic_note": "DRAM bytes per step: bytes per unit from profiles/ncu_traffic.txt x units per step "
-                                "(%.0f rays)" % rays,
+                                "(%.0f rays, %.0f sub-cubes)" % (rays, bricks),
                 "peak_source": "measured (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else
                 "fallback 6800 GB/s",
                 "note": "algorithmic bytes of the stage per step (the first %d timed steps) / its event-timed "
@@ -724,18 +740,17 @@ def run_ours(args):
         # ray from the committed ncu captures times this workload's rays, over
         # the event-timed stage, against one warp instruction per scheduler per
         # cycle (4 per SM) at the SM clock sampled during the timed region
-        ia = traffic_per_unit("k_ray_march", "warp_inst_per_ray")
-        ib = traffic_per_unit("k_ray_shade", "warp_inst_per_ray")
+        pu = raycast_per_unit("warp_inst")
         mhz = (clocks or {}).get("sm_mhz")
-        if ia is not None and ib is not None and mhz:
+        if pu is not None and mhz:
             sms = torch.cuda.get_device_properties(local).multi_processor_count
-            got = (ia + ib) * rays / (stage_sum[dom_i] / len(stage_steps) * 1e-3)
+            got = (pu[0] * rays + pu[1] * bricks) / (stage_sum[dom_i] / len(stage_steps) * 1e-3)
             top = 4.0 * sms * mhz * 1e6
             roofline["issue"] = {"achieved": got, "peak": top, "unit": "warp instructions/s", "frac": got / top,
-                                 "warp_inst_per_ray": ia + ib,
-                                 "note": "warp instructions per ray from profiles/ncu_traffic.txt x %.0f rays per "
-                                         "step / the stage's event time; peak = 4 x %d SMs x %.0f MHz" %
-                                         (rays, sms, mhz)}
+                                 "warp_inst_per_ray": pu[0], "warp_inst_per_subcube": pu[1],
+                                 "note": "warp instructions per ray and per sub-cube from profiles/ncu_traffic.txt x "
+                                         "%.0f rays and %.0f sub-cubes per step / the stage's event time; peak = 4 x "
+                                         "%d SMs x %.0f MHz" % (rays, bricks, sms, mhz)}
 
     cpu = ate = None
     if not args.no_cpu:
@@ -1053,10 +1068,9 @@ def run_plain_vga(args):
     rays = sum(level_pixels(cfg))
     traffic = None
     if dom == "raycast":
-        a_, b_ = traffic_per_unit("k_ray_march", "dram_bytes_per_ray"), traffic_per_unit("k_ray_shade",
-                                                                                          "dram_bytes_per_ray")
-        if a_ is not None and b_ is not None:
-            traffic = (a_ + b_) * rays
+        pu = raycast_per_unit("dram_bytes")
+        if pu is not None:
+            traffic = pu[0] * rays + pu[1] * level_bricks(cfg)
     elif dom == "track":
         px = traffic_per_unit("k_icp_iter", "dram_bytes_per_pixel")
         if px is not None:
@@ -1096,7 +1110,7 @@ def run_plain_vga(args):
             "config": vga_config_json(args, world),
             "latency_ms": {"p50": pct(frame_ms, 50), "p99": pct(frame_ms, 99), "max": float(frame_ms.max())},
             "stages_ms": {n_: float(v) for n_, v in zip(names, stage_mean)},
-            "roofline": {"bound": "hbm", "kernel": {"raycast": "k_ray_march+k_ray_shade", "track": "k_icp_iter",
+            "roofline": {"bound": "hbm", "kernel": {"raycast": "k_band_xy+k_band_z+k_ray_fused", "track": "k_icp_iter",
                                                     "integrate": "k_integrate", "filter": "k_bilateral_batch"}[dom],
                          "stage": dom, "achieved": achieved[dom], "peak": peak, "unit": "GB/s",
                          "frac": achieved[dom] / peak, "traffic": traffic,

@@ -406,8 +406,10 @@ int vs_batch_get_stage_times(vs_batch* b, float* ms);
 int vs_batch_kernels_per_step(vs_batch* b);
 
 /* Launch shape of a runner's steps: a warp's 32 rays form a
- * (1 << ray_tile_log2) x (32 >> ray_tile_log2) pixel tile, and the march /
- * shading grids hold that many 128-thread blocks per SM (0: as many as fit);
+ * (1 << ray_tile_log2) x (32 >> ray_tile_log2) pixel tile, and the ray-cast
+ * grid (march and shading in one launch; colour sessions: the march grid,
+ * then the shading grid) holds that many 128-thread blocks per SM (0: as
+ * many as fit);
  * the bilateral filter and the sub-cube activation work on 32 x
  * bilateral_rows pixel tiles (4, 8 or 16; 0: 8); the integration's update
  * grid holds integrate_blocks_per_sm 256-thread blocks per SM (0: as many as

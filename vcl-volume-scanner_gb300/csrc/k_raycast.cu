@@ -3,16 +3,19 @@
 // Reference: g_rmi_Render_Maps_for_ICP, d_crtc_Cast_Ray_on_TSDF_Cube_NEW,
 // d_gtvu / d_gtvi and d_csnt (STAC/Engine/GPU/z_yooji_cuda_tsdf_renderer.cu:
 // 1069-1209, 466-635, 68-153, 288-464; host set-up :1642-1700).  The
-// reference launches one 16x16-block grid per pyramid level; here two
-// persistent launches cover every level of every session of a batch table:
-// k_ray_march marches each ray to its surface point and k_ray_shade computes
-// the surface normal and writes the maps.  Split, each kernel needs far fewer
-// registers than the fused loop, so more warps hide the gather latency.  Each
-// warp takes 8x4-ray tiles from an atomic work counter, so a slow tile near a
-// surface holds up neither a grid row nor the other warps of its block.  A
-// ray keeps its whole march state in registers, and every voxel read is one
-// 32-bit word that carries both the TSDF value and the weight (one gather
-// instead of the reference's separate float and uchar arrays).
+// reference launches one 16x16-block grid per pyramid level; here one
+// persistent launch (k_ray_fused) covers every level of every session of a
+// batch table, marching each ray to its surface point and computing the
+// surface normal and the maps there.  Colour ray-casts, whose shading needs
+// more registers, run as two launches: k_ray_march writes the surface points
+// to a hit buffer and k_ray_shade shades them.  Each warp takes 8x4-ray tiles
+// from an atomic work counter, so a slow tile near a surface holds up neither
+// a grid row nor the other warps of its block.  A ray keeps its whole march
+// state in registers, and every voxel read is one 32-bit word that carries
+// both the TSDF value and the weight (one gather instead of the reference's
+// separate float and uchar arrays).  Before the march, the distance field of
+// the band sub-cubes is rebuilt (k_band_xy, k_band_z), which lets the march
+// jump through free space.
 //
 // The reference's march loop has no iteration bound: a fine-search ray whose
 // signed steps keep changing direction never leaves it.  The loop here ends
@@ -532,34 +535,40 @@ __global__ void __launch_bounds__(kBandThreads) k_band_z(const BatchTable* __res
 #define VS_SHADE_MIN_BLOCKS 8
 #endif
 
+// the ray of pixel (x, y) of level l to its surface point pg (global
+// coordinates); false: no hit
+template <class S, bool SCENE>
+__device__ inline bool march_ray(const RayArgs& a, const Vol<S>& V, const SessionDev& s, int l, int x, int y, F3& pg) {
+  const bool ext = a.level >= 0;
+  const float* Tcg_in = ext ? a.Tcg : s.pose->Tcg;
+  const float* cen = ext ? a.center : s.pose->center;
+  float Tcg[12], K[4];
+#pragma unroll
+  for (int k = 0; k < 12; k++) Tcg[k] = Tcg_in[k];
+#pragma unroll
+  for (int k = 0; k < 4; k++) K[k] = s.lv[l].K[k];
+  const F3 cam = f3(cen[0], cen[1], cen[2]);
+  // host-side set-up of rmi_Render_Maps_for_ICP (:1667-1675)
+  const F3 cc = f3(s.cube_center[0], s.cube_center[1], s.cube_center[2]);
+  const F3 vcc = sub(cc, cam);
+  const F3 ncc = normalised(vcc);
+  const float dist_cc = length(vcc);
+  const float theta_max = asinf(s.r_cube / dist_cc);
+  // object mode (d_crtc_NEW, :466-635): the segment of the ray through the
+  // cube's bounding sphere inside its view cone; scene mode (d_crtcs,
+  // :908-1066): from the camera centre to 2 r_cube, no cone
+  const float dmin = SCENE ? 0.0f : dist_cc - s.r_cube;
+  const float dmax = SCENE ? 2.0f * s.r_cube : dist_cc + s.r_cube;
+  return cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, dmin, dmax, !SCENE, ncc, theta_max, pg);
+}
+
 // phase 1: march every ray to its surface point (global coordinates; w = 1
 // hit, 0 none) in the session's hit buffer
 template <class S, bool SCENE>
 __global__ void __launch_bounds__(kRayThreads, VS_RAY_MIN_BLOCKS) k_ray_march(RayArgs a) {
   for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
-    const Vol<S> V = volume_of<S>(s);
-    const bool ext = a.level >= 0;
-    const float* Tcg_in = ext ? a.Tcg : s.pose->Tcg;
-    const float* cen = ext ? a.center : s.pose->center;
-    float Tcg[12], K[4];
-#pragma unroll
-    for (int k = 0; k < 12; k++) Tcg[k] = Tcg_in[k];
-#pragma unroll
-    for (int k = 0; k < 4; k++) K[k] = s.lv[l].K[k];
-    const F3 cam = f3(cen[0], cen[1], cen[2]);
-    // host-side set-up of rmi_Render_Maps_for_ICP (:1667-1675)
-    const F3 cc = f3(s.cube_center[0], s.cube_center[1], s.cube_center[2]);
-    const F3 vcc = sub(cc, cam);
-    const F3 ncc = normalised(vcc);
-    const float dist_cc = length(vcc);
-    const float theta_max = asinf(s.r_cube / dist_cc);
     F3 pg;
-    // object mode (d_crtc_NEW, :466-635): the segment of the ray through the
-    // cube's bounding sphere inside its view cone; scene mode (d_crtcs,
-    // :908-1066): from the camera centre to 2 r_cube, no cone
-    const float dmin = SCENE ? 0.0f : dist_cc - s.r_cube;
-    const float dmax = SCENE ? 2.0f * s.r_cube : dist_cc + s.r_cube;
-    const bool hit = cast_ray(V, s, K, (float)x, (float)y, Tcg, cam, dmin, dmax, !SCENE, ncc, theta_max, pg);
+    const bool hit = march_ray<S, SCENE>(a, volume_of<S>(s), s, l, x, y, pg);
     s.ray_hit[hit_offset(s, l) + (size_t)y * s.lv[l].W + x] =
         hit ? make_float4(pg.x, pg.y, pg.z, 1.0f) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   });
@@ -626,60 +635,81 @@ __device__ uint32_t nearest_color(const Vol<S>& V, const SessionDev& s, F3 pg) {
   return __ldg(s.col + w);
 }
 
-// phase 2: surface normal of every hit (d_csnt), camera-frame vertex and
-// normal, shading, colour, into the model maps or the external outputs
+// surface normal of a hit (d_csnt), camera-frame vertex and normal, shading,
+// colour, into the model maps or the external outputs
+template <class S, bool COLOR>
+__device__ inline void shade_ray(const RayArgs& a, const Vol<S>& V, const SessionDev& s, int l, int x, int y,
+                                 bool hit, F3 pg) {
+  const bool ext = a.level >= 0;
+  const size_t idx = (size_t)y * s.lv[l].W + x;
+  F3 sn;
+  bool valid = hit;
+  if (valid) valid = surface_normal(V, s, pg, sn);
+  float dep = 0.0f, img = 0.0f;
+  uint32_t rgb = 0u;
+  F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
+  if (valid) {
+    if (COLOR && s.col) rgb = (a.mode & kRayNearestColor) ? nearest_color(V, s, pg) : trilinear_color(V, s, pg);
+    const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
+    float Tgc[12];
+#pragma unroll
+    for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k];
+    pc = transform(pg, Tgc);
+    dep = pc.z;
+    sc = (a.mode & kRayGlobalNormals) ? sn : rotate(sn, Tgc);
+    float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
+    img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
+  }
+  if (ext) {
+    if (!valid && (a.mode & kRayWhiteBackground)) rgb = 0x00ffffffu;
+    a.out_depth[idx] = dep;
+    if (a.out_vtx3) {
+      a.out_vtx3[3 * idx] = pc.x;
+      a.out_vtx3[3 * idx + 1] = pc.y;
+      a.out_vtx3[3 * idx + 2] = pc.z;
+    }
+    a.out_nrm3[3 * idx] = sc.x;
+    a.out_nrm3[3 * idx + 1] = sc.y;
+    a.out_nrm3[3 * idx + 2] = sc.z;
+    if (a.out_img) a.out_img[idx] = (uint8_t)img;
+    if (COLOR && a.out_rgb) {
+      const size_t plane = (size_t)s.lv[l].W * s.lv[l].H;
+      a.out_rgb[idx] = (uint8_t)rgb_channel(rgb, 0);
+      a.out_rgb[plane + idx] = (uint8_t)rgb_channel(rgb, 1);
+      a.out_rgb[2 * plane + idx] = (uint8_t)rgb_channel(rgb, 2);
+    }
+  } else {
+    const float vw = valid ? 1.0f : 0.0f;
+    s.m_depth[l][idx] = dep;
+    s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
+    s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
+    s.m_img[l][idx] = (uint8_t)img;
+    if (COLOR && s.col) s.m_rgb[l][idx] = rgb;
+  }
+}
+
+// phase 2: the maps of every ray from its surface point in the hit buffer
 template <class S, bool COLOR>
 __global__ void __launch_bounds__(kRayThreads, VS_SHADE_MIN_BLOCKS) k_ray_shade(RayArgs a) {
   for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
+    const float4 h = s.ray_hit[hit_offset(s, l) + (size_t)y * s.lv[l].W + x];
+    shade_ray<S, COLOR>(a, volume_of<S>(s), s, l, x, y, h.w != 0.0f, f3(h.x, h.y, h.z));
+  });
+}
+
+#ifndef VS_FUSED_MIN_BLOCKS
+#define VS_FUSED_MIN_BLOCKS 8
+#endif
+
+// both phases in one pass, without the hit buffer (every ray-cast without
+// colour)
+template <class S, bool SCENE>
+__global__ void __launch_bounds__(kRayThreads, VS_FUSED_MIN_BLOCKS) k_ray_fused(RayArgs a) {
+  for_each_ray_tile(a, [&](const SessionDev& s, int l, int x, int y) {
     const Vol<S> V = volume_of<S>(s);
-    const bool ext = a.level >= 0;
-    const size_t idx = (size_t)y * s.lv[l].W + x;
-    const float4 h = s.ray_hit[hit_offset(s, l) + idx];
-    const F3 pg = f3(h.x, h.y, h.z);
-    F3 sn;
-    bool valid = h.w != 0.0f;
-    if (valid) valid = surface_normal(V, s, pg, sn);
-    float dep = 0.0f, img = 0.0f;
-    uint32_t rgb = 0u;
-    F3 pc = f3(-100.0f, -100.0f, -100.0f), sc = f3(-100.0f, -100.0f, -100.0f);
-    if (valid) {
-      if (COLOR && s.col) rgb = (a.mode & kRayNearestColor) ? nearest_color(V, s, pg) : trilinear_color(V, s, pg);
-      const float* Tgc_in = ext ? a.Tgc : s.pose->Tgc;
-      float Tgc[12];
-#pragma unroll
-      for (int k = 0; k < 12; k++) Tgc[k] = Tgc_in[k];
-      pc = transform(pg, Tgc);
-      dep = pc.z;
-      sc = (a.mode & kRayGlobalNormals) ? sn : rotate(sn, Tgc);
-      float ang = sc.x * a.light[0] + sc.y * a.light[1] + sc.z * a.light[2];
-      img = fmaxf(0.0f, fminf(255.0f, (0.8f * ang + 0.2f) * 255.0f));
-    }
-    if (ext) {
-      if (!valid && (a.mode & kRayWhiteBackground)) rgb = 0x00ffffffu;
-      a.out_depth[idx] = dep;
-      if (a.out_vtx3) {
-        a.out_vtx3[3 * idx] = pc.x;
-        a.out_vtx3[3 * idx + 1] = pc.y;
-        a.out_vtx3[3 * idx + 2] = pc.z;
-      }
-      a.out_nrm3[3 * idx] = sc.x;
-      a.out_nrm3[3 * idx + 1] = sc.y;
-      a.out_nrm3[3 * idx + 2] = sc.z;
-      if (a.out_img) a.out_img[idx] = (uint8_t)img;
-      if (COLOR && a.out_rgb) {
-        const size_t plane = (size_t)s.lv[l].W * s.lv[l].H;
-        a.out_rgb[idx] = (uint8_t)rgb_channel(rgb, 0);
-        a.out_rgb[plane + idx] = (uint8_t)rgb_channel(rgb, 1);
-        a.out_rgb[2 * plane + idx] = (uint8_t)rgb_channel(rgb, 2);
-      }
-    } else {
-      const float vw = valid ? 1.0f : 0.0f;
-      s.m_depth[l][idx] = dep;
-      s.m_vtx[l][idx] = make_float4(pc.x, pc.y, pc.z, vw);
-      s.m_nrm[l][idx] = make_float4(sc.x, sc.y, sc.z, vw);
-      s.m_img[l][idx] = (uint8_t)img;
-      if (COLOR && s.col) s.m_rgb[l][idx] = rgb;
-    }
+    F3 pg;
+    const bool hit = march_ray<S, SCENE>(a, V, s, l, x, y, pg);
+    shade_ray<S, false>(a, V, s, l, x, y, hit, pg);
   });
 }
 
@@ -730,6 +760,14 @@ void launch_ray_phases(const RayArgs& a0, const LaunchShape& shape, bool color, 
   RayArgs a = a0;
   k_band_xy<<<sm_count() * 2, kBandThreads, 0, st>>>(a.bt);
   k_band_z<<<sm_count() * 2, kBandThreads, 0, st>>>(a.bt);
+  if (!color) {
+    static const int most_fused = max_per_sm(k_ray_fused<S, false>);
+    if (a.mode & kRayScene)
+      k_ray_fused<S, true><<<grid_of(shape.march_blocks_per_sm, most_fused), kRayThreads, 0, st>>>(a);
+    else
+      k_ray_fused<S, false><<<grid_of(shape.march_blocks_per_sm, most_fused), kRayThreads, 0, st>>>(a);
+    return;
+  }
   if (a.mode & kRayScene)
     k_ray_march<S, true><<<grid_of(shape.march_blocks_per_sm, ray_max_per_sm<S>(false)), kRayThreads, 0, st>>>(a);
   else
