@@ -49,14 +49,14 @@ struct RayArgs {
   int mode;             // kRay* bits of the external render variants (0: the ICP maps)
 };
 
-// Volume reads.  A brick whose occupancy bit is clear has weight 0 in every
-// voxel (weights only grow), so its voxels answer "no value" from a 32 KB
-// bitmap that stays in L1 instead of a volume gather, with results identical
-// to reading the voxel.
+// Volume reads.  Every voxel read is one word (TSDF value and weight); a
+// voxel never written holds weight 0 and reads "no value".  Free space is
+// skipped through the band distance field, so the samples the march does take
+// lie near band bricks, where a separate occupancy test would only add
+// instructions.
 template <class S>
 struct Vol {
   const typename S::word* v;
-  const uint32_t* occ;
   const uint8_t* bdist;  // distance in bricks to the nearest band brick
   int dim[3];
   uint32_t nbx, nbxy;  // bricks per row / per slab
@@ -68,8 +68,7 @@ struct Vol {
   __device__ inline uint32_t wx(int x) const { return (((uint32_t)x >> 3) << 9) + ((uint32_t)x & 7u); }
   __device__ inline uint32_t wy(int y) const { return ((uint32_t)y >> 3) * sy + (((uint32_t)y & 7u) << 3); }
   __device__ inline uint32_t wz(int z) const { return ((uint32_t)z >> 3) * sz + (((uint32_t)z & 7u) << 6); }
-  // the value of word i, and whether its weight is > 0 (a voxel of an
-  // unoccupied brick has weight 0, so the weight alone decides)
+  // the value of word i, and whether its weight is > 0
   __device__ inline bool word_ok(uint32_t i, float& t) const {
     uint32_t w;
     S::decode(__ldg(v + i), t, w);
@@ -91,7 +90,7 @@ struct Vol {
   // never changes a sample).  A NaN coordinate fails every comparison below
   // and gives 0.
   static constexpr int kMaxRun = 4096;
-  static constexpr int kMaxBoxes = 3;
+  static constexpr int kMaxBoxes = 2;
   __device__ inline int free_run(F3 p, F3 inc) const {
     const float d = 0.05f;
     const float pa[3] = {p.x, p.y, p.z}, ia[3] = {inc.x, inc.y, inc.z};
@@ -166,8 +165,6 @@ struct Vol {
     const int x = (int)(p.x + 0.5f), y = (int)(p.y + 0.5f), z = (int)(p.z + 0.5f);
     if (x >= dim[0] || y >= dim[1] || z >= dim[2]) return false;
     const uint32_t i = wx(x) + wy(y) + wz(z);
-    // brick index = i / 512
-    if (!((__ldg(occ + (i >> 14)) >> ((i >> 9) & 31u)) & 1u)) return false;
     float t;
     if (!word_ok(i, t)) return false;
     out = t;
@@ -440,7 +437,6 @@ template <class S>
 __device__ inline Vol<S> volume_of(const SessionDev& s) {
   Vol<S> V;
   V.v = reinterpret_cast<const typename S::word*>(s.vol);
-  V.occ = s.occ;
   V.bdist = s.bdist;
   for (int k = 0; k < 3; k++) V.dim[k] = s.dim[k];
   V.nbx = (uint32_t)s.nb[0];
