@@ -1176,6 +1176,21 @@ def _solve_f32_refined(A, b, steps=2):
     return x
 
 
+def _device_inverse(T64):
+    """the float camera-to-global pose a session integrates with: the rigid
+    inverse of its FP64 pose in FP64, in the device's operation order,
+    rounded to float (a float inversion of the float pose differs in the last
+    bits, enough to move a sub-cube across the activation boundary)"""
+    T = np.asarray(T64, np.float64)
+    out = np.zeros((4, 4), np.float64)
+    for r in range(3):
+        for c in range(3):
+            out[r, c] = T[c, r]
+        out[r, 3] = -(float(T[0, r]) * float(T[0, 3]) + float(T[1, r]) * float(T[1, 3]) + float(T[2, r]) * float(T[2, 3]))
+    out[3, 3] = 1.0
+    return out.astype(np.float32)
+
+
 def _rot_err(A, B):
     R = np.asarray(A, np.float64)[:3, :3].T @ np.asarray(B, np.float64)[:3, :3]
     w = np.array([R[2, 1] - R[1, 2], R[0, 2] - R[2, 0], R[1, 0] - R[0, 1]]) / 2.0
@@ -1305,7 +1320,7 @@ def run_precision(args):
                 poses.append(s.pose()[1])
                 if before is not None:
                     Tg = np.ascontiguousarray(s.pose()[0], np.float32)
-                    Tc = O.pose_inverse(Tg)
+                    Tc = _device_inverse(s.pose()[1])
                     vol = O.Volume(ocfg32)
                     vol.set(*before)
                     vol.integrate(O.depth_to_m(depth[k]), Tg, Tc)
@@ -1315,7 +1330,7 @@ def run_precision(args):
                     if upd.any():
                         tsdf_steps.append(float(np.max(np.abs(t_[upd].astype(np.float64) - ot[upd])) * 32767.0))
                     vol.set(t_, w_)
-                    od, ov, _, _ = vol.raycast(0, Tg, Tc, O.camera_center(Tg), light)
+                    od, ov, _, _ = vol.raycast(0, Tg, Tc, np.ascontiguousarray(Tc[:3, 3]), light)
                     m0 = s.maps(0)
                     gv, gd = m0["model_vertex"].reshape(-1, 3), m0["model_depth"].reshape(-1)
                     both = (od.reshape(-1) > 0) & (gd > 0)

@@ -78,20 +78,21 @@ __device__ inline bool interp(const Taps& t, float4 a, float4 b, float4 c, float
 
 // d_cssfp_Compute_Single_Summand_with_Forward_Params.  Two rounds of reads:
 // the pixel's depth (and input normal), then the eight model-map taps.
-// K: fx, fy, cx, cy, 1/fx, 1/fy.  The reference's four divisions per pixel
-// (back-projection by fx and fy, projection by z twice) become products with
-// the inverse focal lengths and one reciprocal of z, and the normal's
-// 1/|n| a reciprocal square root: a few ulps on the per-pixel terms, which
-// move a well-posed frame's pose by ~1e-7, far inside the tolerance.
+// The per-pixel arithmetic is the reference's, operation for operation
+// (IEEE divisions and square root): every pixel's term, and therefore every
+// correspondence decision at the distance threshold, equals the float
+// oracle's.  (Products with inverse focal lengths, one reciprocal of z and a
+// reciprocal square root were 4 % faster, but moved the correspondence set
+// of frames whose pixels sit on the threshold, up to 3.5e-4 rad per frame.)
 __device__ inline bool icp_term(int x, int y, int w, int h, const float* K, float d1, float4 q,
                                 const float4* __restrict__ mvtx, const float4* __restrict__ mnrm, const float* T21,
                                 float th_icp, float cos_normal, float A[6], float& b) {
   const bool ntest = cos_normal > -2.0f;
   if (d1 < 1.0e-6f) return false;
-  const F3 tp = f3(d1 * ((float)x - K[2]) * K[4], d1 * ((float)y - K[3]) * K[5], d1);
+  F3 tp = back_project((float)x, (float)y, K, d1);
   F3 p1 = transform(tp, T21);
-  const float rz = 1.0f / p1.z;
-  const float u = K[0] * p1.x * rz + K[2], v = K[1] * p1.y * rz + K[3];
+  float u, v;
+  project(p1, K, u, v);
   Taps t;
   if (!tap_setup(u, v, w, h, t)) return false;
   const float4 va = __ldg(mvtx + t.i00), vb = __ldg(mvtx + t.i01), vc = __ldg(mvtx + t.i10), vd = __ldg(mvtx + t.i11);
@@ -102,8 +103,7 @@ __device__ inline bool icp_term(int x, int y, int w, int h, const float* K, floa
   const float4 na = __ldg(mnrm + t.i00), nb = __ldg(mnrm + t.i01), nc = __ldg(mnrm + t.i10), nd = __ldg(mnrm + t.i11);
   F3 n;
   if (!interp(t, na, nb, nc, nd, n)) return false;
-  const float inrm = rsqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
-  n = f3(n.x * inrm, n.y * inrm, n.z * inrm);
+  n = normalised(n);
   if (ntest) {
     if (q.w == 0.0f) return false;
     F3 nin = rotate(f3(q.x, q.y, q.z), T21);
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
   __shared__ PT wsum[kThreads / 32][29];
   __shared__ int s_last, s_item;
   __shared__ double fin[29];
-  __shared__ float sT21[12], sK[6];
+  __shared__ float sT21[12], sK[4];
   const int n = bt->n;
   const int* pre = bt->icp[level];
   const int total = pre[n];
@@ -567,7 +567,6 @@ __global__ void __launch_bounds__(kThreads, VS_ICP_MIN_BLOCKS)
     // which leaves the registers to the 29 running sums
     if (threadIdx.x < 12) sT21[threadIdx.x] = P->T21[threadIdx.x];
     if (threadIdx.x < 4) sK[threadIdx.x] = s->lv[level].K[threadIdx.x];
-    if (threadIdx.x == 4 || threadIdx.x == 5) sK[threadIdx.x] = 1.0f / s->lv[level].K[threadIdx.x - 4];
     __syncthreads();
     const float* K = sK;
     const float* T21 = sT21;
