@@ -440,17 +440,19 @@ def _ate_worker_init():
 
 def _ate_worker(job):
     """oracle poses and tracked flags of one session over frames 0..n-1: the
-    FP64 pipeline, or (fp32=True) the float pipeline in the benchmark's own
-    arithmetic choices (compensated sums, int16 TSDF)"""
+    FP64 pipeline, or (job[2] = (reduction mode, TSDF storage)) the float
+    pipeline with those arithmetic choices; (2, 1), compensated sums and int16
+    TSDF, are the benchmark's own"""
     spec, n = job[0], job[1]
-    fp32 = len(job) > 2 and job[2]
+    variant = job[2] if len(job) > 2 else None
+    fp32 = variant is not None
     import oracle_py as O
 
     O.load()
     set_omp_threads(1)
     depth, gt, centre = generate(spec, n, oracle=True)
     if fp32:
-        s = O.Session(oracle_config(spec, centre, reduce_mode=2, tsdf_store=1), f64=False)
+        s = O.Session(oracle_config(spec, centre, reduce_mode=variant[0], tsdf_store=variant[1]), f64=False)
     else:
         s = O.Session(oracle_config(spec, centre, reduce_mode=3, tsdf_store=0), f64=True)
     poses, tracked = [], []
@@ -469,8 +471,8 @@ def ate_all_sessions(specs, ours, ours_tracked, warm_depth, steps):
     jobs = [(sp, len(ours[i])) for i, sp in enumerate(specs)]
     t0 = time.perf_counter()
     ctx = mp.get_context("spawn")
-    with ctx.Pool(max(1, os.cpu_count() or 1), initializer=_ate_worker_init) as pool:
-        ref = pool.map(_ate_worker, jobs, chunksize=1)
+    pool = ctx.Pool(max(1, os.cpu_count() or 1), initializer=_ate_worker_init)
+    ref = pool.map(_ate_worker, jobs, chunksize=1)
     dt = time.perf_counter() - t0
     per, worst, worst_i, worst_frame, all_rms = {}, 0.0, None, 0.0, 0.0
     lost_gpu, lost_oracle, sq, n_timed = {}, {}, 0.0, 0
@@ -502,18 +504,32 @@ def ate_all_sessions(specs, ours, ours_tracked, warm_depth, steps):
                    "trajectories start at the identity); the FP64 oracle runs every frame from frame 0" %
                    (warm_depth, warm_depth + steps - 1)}
     if worst_i is not None:
-        # how sensitive that session is: the float oracle (the same arithmetic
-        # choices as the GPU path, run step by step) against the FP64 one,
-        # and the FP64 pipeline against the generator's ground truth
-        fp, _, gt = _ate_worker((specs[worst_i], len(ours[worst_i]), True))
+        # how sensitive that session is: the float oracle, run step by step in
+        # every combination of the reference's arithmetic choices (reduction:
+        # the reference's tree, plain, compensated, FP64 sums; TSDF: float,
+        # int16), against the FP64 one, and the FP64 pipeline against the
+        # generator's ground truth.  A session whose float variants spread
+        # over more than the 1 mm bound bifurcates: the rounding of any float
+        # implementation decides which way its trajectory goes.
+        n_w = len(ours[worst_i])
+        variants = [(rm, ts) for rm in (0, 1, 2, 3) for ts in (0, 1)]
+        fl = pool.map(_ate_worker, [(specs[worst_i], n_w, v) for v in variants], chunksize=1)
         rp = ref[worst_i][0]
-        dfl = np.linalg.norm(centres(fp) - centres(rp), axis=1)[warm_depth:] * 1e3
+        gt = fl[0][2]
+        spread = {}
+        for v, (fp, _, _) in zip(variants, fl):
+            dfl = np.linalg.norm(centres(fp) - centres(rp), axis=1)[warm_depth:] * 1e3
+            spread["%s_%s" % (("reference_tree", "plain", "compensated", "fp64_sums")[v[0]],
+                              ("float", "int16")[v[1]])] = round(float(np.sqrt(np.mean(dfl ** 2))), 4)
         dgt = np.linalg.norm(centres(rp) - centres(gt), axis=1) * 1e3
         out["worst_session"] = {"session": worst_i, "size": "%dx%d" % (specs[worst_i]["w"], specs[worst_i]["h"]),
                                 "volume": specs[worst_i]["dim"], "gpu_rms_mm": worst,
-                                "fp32_oracle_vs_fp64_rms_mm": float(np.sqrt(np.mean(dfl ** 2))),
-                                "fp32_oracle_vs_fp64_max_mm": float(dfl.max()),
+                                "fp32_oracle_vs_fp64_rms_mm": spread["compensated_int16"],
+                                "float_oracle_variants_vs_fp64_rms_mm": spread,
+                                "float_variants_beyond_1mm": int(sum(1 for x in spread.values() if x >= 1.0)),
                                 "fp64_vs_ground_truth_rms_mm": float(np.sqrt(np.mean(dgt ** 2)))}
+    pool.close()
+    pool.join()
     return out
 
 
