@@ -157,11 +157,17 @@ def test_color_frames_leave_tracking_unchanged_and_batch_equals_alone(gpu, ccase
         col_alone = a.color_volume()
         map_alone = a.color_map(0)
         assert (map_alone[0][a.maps(0)["model_depth"] > 0] > 0).mean() > 0.9
+        plain_pose, plain_maps = p.pose()[1], [p.maps(l)["model_vertex"] for l in range(plain.levels)]
+    # a batch holding colour sessions and a session without colour: the colour
+    # ray-cast's two launches serve all three, each as alone
     other = color_case(width=320, height=240, dim=64, size=1.0, frames=4, seed=6)
-    with V.Session(cfg) as a, V.Session(other["cfg"]) as b, V.Batch() as batch:
+    with V.Session(cfg) as a, V.Session(other["cfg"]) as b, V.Session(plain) as q, V.Batch() as batch:
         for k in range(4):
             a.set_color_frame(ccase["rgb"][k])
             b.set_color_frame(other["rgb"][k])
-            batch.step_host([a, b], [ccase["depth"][k], other["depth"][k]])
+            batch.step_host([a, b, q], [ccase["depth"][k], other["depth"][k], ccase["depth"][k]])
         assert np.array_equal(a.color_volume(), col_alone)
         assert np.array_equal(a.color_map(0), map_alone)
+        assert np.array_equal(q.pose()[1], plain_pose)
+        for l in range(plain.levels):
+            assert np.array_equal(q.maps(l)["model_vertex"], plain_maps[l]), l

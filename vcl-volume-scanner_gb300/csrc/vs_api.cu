@@ -285,9 +285,9 @@ size_t vs_session_bytes(const vs_config* c) {
   }
   b += (size_t)kIcpMaxBlocks * kPartials * 16 + sizeof(Pose) + sizeof(SessionDev) + sizeof(BatchTable) + 64;
   b += (size_t)(c->dim[0] + c->dim[1] + c->dim[2] + w + h) * 4;
+  for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
   b += (size_t)w * h * (4 + 8);                                                // ray-scale map, {depth, scale} map
   if (c->color) {
-    for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 16;  // ray-cast hit points
     b += (size_t)c->dim[0] * c->dim[1] * c->dim[2] * 4 + (size_t)w * h * (3 + 4);  // colour volume and frame
     for (int l = 0; l < c->levels; l++) b += (size_t)(w >> l) * (h >> l) * 4;      // colour maps
   }
@@ -361,7 +361,8 @@ int vs_session_create(const vs_config* cfg, vs_session** out) {
     rc |= alloc(s, &h.rgb_packed, n0 * 4);
     for (int l = 0; l < h.levels; l++) rc |= alloc(s, &h.m_rgb[l], (size_t)h.lv[l].W * h.lv[l].H * 4);
   }
-  if (cfg->color) {  // the hit buffer between the two launches of a colour ray-cast
+  {  // the hit buffer between the two launches of a colour ray-cast (a batch with a colour
+     // session runs them for every session of the batch)
     size_t npx = 0;
     for (int l = 0; l < h.levels; l++) npx += (size_t)h.lv[l].W * h.lv[l].H;
     rc |= alloc(s, &h.ray_hit, npx * sizeof(float4));

@@ -94,7 +94,8 @@ struct SessionDev {
   // tables built once per session with the reference's formulas
   float* lut_vox;                // voxel centre coordinate per axis: dim[0] + dim[1] + dim[2]
   float* lut_ray;                // level-0 K^-1 [x 1 1] (W) then [1 y 1] (H) components
-  float4* ray_hit;               // colour ray-casts: surface points, every level's pixels in turn
+  float4* ray_hit;               // surface points of a colour ray-cast (two launches), every level's
+                                 // pixels in turn
   // colour (NULL pointers when the session keeps none)
   uint32_t* col;                 // colour bricks parallel to vol: per voxel 0x00BBGGRR
   uint8_t* rgb_in;               // level-0 colour frame, planar R, G, B
