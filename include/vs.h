@@ -390,11 +390,16 @@ int vs_batch_destroy(vs_batch* b);
 /* one frame for each of n (1..VS_MAX_BATCH) distinct sessions.
  * depth_mm_dev[i]: device uint16 frame of session i, or NULL (or a NULL
  * array) when the frame is already in the session's input buffer.  Enqueued
- * on `stream` (NULL: the runner's own stream); returns without waiting. */
+ * on `stream` (NULL: the runner's own stream); returns without waiting.  The
+ * step's first kernel reads each frame in place (no copy), so a frame must
+ * not change until the step is done (work enqueued after it on the same
+ * stream is ordered after it). */
 int vs_batch_step(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_dev,
                   void* stream);
 /* host frames in, poses out (T_gc_out: n x 16 floats, tracked_out: n ints,
- * either may be NULL); returns when the step has finished */
+ * either may be NULL); returns when the step has finished.  A frame in pinned
+ * host memory (cudaHostAlloc / cudaHostRegister) is read in place by the
+ * step's first kernel over the host link; a pageable one is copied first. */
 int vs_batch_step_host(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_host,
                        float* T_gc_out, int* tracked_out);
 int vs_batch_sync(vs_batch* b);

@@ -113,6 +113,25 @@ def test_batch_device_frames_and_async_step(cases, alone):
             s.close()
 
 
+def test_batch_pinned_host_frames_read_in_place(cases, alone):
+    """pinned host frames are read by the step's first kernel over the host
+    link, pageable ones copied first: the same results either way"""
+    sessions = [V.Session(c["cfg"]) for c in cases]
+    try:
+        with V.Batch() as b:
+            for k in range(2):
+                pinned = [torch.from_numpy(c["depth"][k].view(np.int16)).pin_memory() for c in cases]
+                frames = [p.numpy().view(np.uint16) for p in pinned]
+                if k == 1:
+                    frames[1] = np.array(cases[1]["depth"][k])  # one pageable frame in the mix
+                b.step_host(sessions, frames)
+                for i, s in enumerate(sessions):
+                    _assert_same(_snapshot(s), alone[i][k], "pinned frames, session %d frame %d" % (i, k))
+    finally:
+        for s in sessions:
+            s.close()
+
+
 def test_full_batch_of_small_sessions(gpu):
     """VS_MAX_BATCH sessions in one step; a few are checked against their run alone"""
     case = helpers.make_case(width=64, height=48, dim=32, size=1.0, frames=2, seed=13)

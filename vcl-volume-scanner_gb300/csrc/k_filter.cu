@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(BX* R) k_bilateral_batch(const BatchTable* __r
     const int W = s->lv[0].W, H = s->lv[0].H;
     const int tw = (W + BX - 1) / BX;
     const float g[5] = {s->gauss[0], s->gauss[1], s->gauss[2], s->gauss[1], s->gauss[0]};
-    bilateral_tile<true, R>(m, s->depth_mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
+    const uint16_t* __restrict__ mm = bt->frame[slot] ? bt->frame[slot] : s->depth_mm;
+    bilateral_tile<true, R>(m, mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
                             (t / tw) * R, g, s->lam_map ? s->dl_map : nullptr, s->lam_map);
     if (s->rgb_packed) {
       // the colour frame as one word per pixel, for the integration's gathers

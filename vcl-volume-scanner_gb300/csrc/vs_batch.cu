@@ -204,8 +204,11 @@ int check_sessions(vs_batch* b, vs_session* const* ss, int n, Schedule& k) {
   return VS_OK;
 }
 
-// fills the next ring slot's table and launches; the frames are already in place
-int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cudaStream_t st, int r) {
+// fills the next ring slot's table and launches.  frames (may be NULL): per
+// session the frame its ingest reads in place (device memory or device-
+// addressable pinned host memory; a NULL entry: the session's own buffer)
+int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cudaStream_t st, int r,
+                const uint16_t* const* frames = nullptr) {
   if (!b->exec[0] || !b->sched.covers(k)) {
     Schedule m = k;
     if (b->exec[0] && b->sched.reduce_mode == k.reduce_mode && b->sched.tsdf_type == k.tsdf_type &&
@@ -230,6 +233,7 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
     dr[i] = ss[i]->d;
   }
   fill_batch_table(*b->h_tab[r], hr, dr, n, b->shape.ray_lx, b->shape.bil_rows);
+  for (int i = 0; i < n; i++) b->h_tab[r]->frame[i] = frames ? frames[i] : nullptr;
   // ICP groups: largest sessions first, each to the group with fewer pixels
   int order[kMaxSlots];
   for (int i = 0; i < n; i++) order[i] = i;
@@ -237,6 +241,7 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
   std::stable_sort(order, order + n, [&](int a, int c) { return px(a) > px(c); });
   const SessionDev* gh[kIcpGroups][kMaxSlots];
   const SessionDev* gd[kIcpGroups][kMaxSlots];
+  const uint16_t* gf[kIcpGroups][kMaxSlots];
   int gn[kIcpGroups] = {0};
   long long load[kIcpGroups] = {0};
   for (int q = 0; q < n; q++) {
@@ -246,11 +251,14 @@ int launch_step(vs_batch* b, vs_session* const* ss, int n, const Schedule& k, cu
       if (load[j] < load[g]) g = j;
     gh[g][gn[g]] = hr[i];
     gd[g][gn[g]] = dr[i];
+    gf[g][gn[g]] = frames ? frames[i] : nullptr;
     gn[g]++;
     load[g] += px(i);
   }
-  for (int g = 0; g < kIcpGroups; g++)
+  for (int g = 0; g < kIcpGroups; g++) {
     fill_batch_table(b->h_grp[r][g], gh[g], gd[g], gn[g], b->shape.ray_lx, b->shape.bil_rows);
+    for (int j = 0; j < gn[g]; j++) b->h_grp[r][g].frame[j] = gf[g][j];
+  }
   cudaError_t e = cudaGraphLaunch(b->exec[r], st);
   if (e == cudaSuccess) e = cudaEventRecord(b->done[r], st);
   if (e != cudaSuccess) return cuda_fail_code(e, "batch step launch");
@@ -375,15 +383,8 @@ int vs_batch_step(vs_batch* b, vs_session* const* sessions, int n, const uint16_
   int r = 0;
   rc = claim_slot(b, r);
   if (rc) return rc;
-  for (int i = 0; i < n; i++) {
-    const uint16_t* src = depth_mm_dev ? depth_mm_dev[i] : nullptr;
-    const SessionDev& h = sessions[i]->h;
-    if (src && src != h.depth_mm) {
-      cudaError_t e = cudaMemcpyAsync(h.depth_mm, src, (size_t)h.lv[0].W * h.lv[0].H * 2, cudaMemcpyDeviceToDevice, st);
-      if (e != cudaSuccess) return cuda_fail_code(e, "batch frame copy");
-    }
-  }
-  return launch_step(b, sessions, n, k, st, r);
+  // the ingest reads each device frame in place: no copy into the session
+  return launch_step(b, sessions, n, k, st, r, depth_mm_dev);
 }
 
 int vs_batch_step_host(vs_batch* b, vs_session* const* sessions, int n, const uint16_t* const* depth_mm_host,
@@ -395,14 +396,26 @@ int vs_batch_step_host(vs_batch* b, vs_session* const* sessions, int n, const ui
   int r = 0;
   rc = claim_slot(b, r);
   if (rc) return rc;
+  // pinned host frames are read in place by the ingest (the step reads them
+  // over the host link while it runs, and this call returns only after the
+  // step); pageable ones are copied into the session first
+  const uint16_t* direct[kMaxSlots];
   for (int i = 0; i < n; i++) {
     if (!depth_mm_host[i]) return fail_code(VS_ERR_ARG, "null host frame");
+    direct[i] = nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, depth_mm_host[i]) == cudaSuccess && a.type == cudaMemoryTypeHost &&
+        a.devicePointer) {
+      direct[i] = static_cast<const uint16_t*>(a.devicePointer);
+      continue;
+    }
+    cudaGetLastError();  // a pageable pointer may leave an error behind
     const SessionDev& h = sessions[i]->h;
     cudaError_t e = cudaMemcpyAsync(h.depth_mm, depth_mm_host[i], (size_t)h.lv[0].W * h.lv[0].H * 2,
                                     cudaMemcpyHostToDevice, b->stream);
     if (e != cudaSuccess) return cuda_fail_code(e, "batch frame upload");
   }
-  rc = launch_step(b, sessions, n, k, b->stream, r);
+  rc = launch_step(b, sessions, n, k, b->stream, r, direct);
   if (rc) return rc;
   cudaError_t e = cudaEventSynchronize(b->done[r]);
   if (e != cudaSuccess) return cuda_fail_code(e, "batch step");

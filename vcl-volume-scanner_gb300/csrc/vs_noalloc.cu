@@ -56,7 +56,7 @@ namespace {
 
 constexpr size_t kNoAllocMaxBricks = 262144;  // 512^3 voxels in 8^3 sub-cubes
 constexpr size_t kDescBytes = 2048;           // SessionDev record, padded
-constexpr size_t kTableBytes = 4096;          // one-slot BatchTable, padded
+constexpr size_t kTableBytes = 8192;          // one-slot BatchTable, padded
 constexpr size_t kLutBytes = (3 * 1024 + 2 * 2048) * sizeof(float);  // voxel-centre and ray tables
 constexpr size_t kCounterBytes = 256;
 constexpr size_t kHeadBytes = kDescBytes + kTableBytes + kLutBytes + kCounterBytes;
