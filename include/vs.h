@@ -433,8 +433,9 @@ int vs_batch_set_launch_shape(vs_batch* b, const vs_launch_shape* in);
  * volumes and poses; no state changes) under their candidate shapes, reps
  * launches each, and keeps the fastest of each for the runner's later steps:
  * the ray-cast (ray tile and march grid), the filter (tile rows) and the
- * integration (update grid, timed as dry runs that store no voxel).  best
- * and best_ms (ms per ray-cast stage) may be NULL. */
+ * integration (update grid, timed as dry runs that store no voxel); for the
+ * last two a shape other than the default must be more than 3 % faster.
+ * best and best_ms (ms per ray-cast stage) may be NULL. */
 int vs_batch_autotune(vs_batch* b, vs_session* const* sessions, int n, int reps, vs_launch_shape* best,
                       float* best_ms);
 
