@@ -790,7 +790,8 @@ def run_ours(args):
             "roofline": roofline,
             "cpu_baseline": cpu,
             "e2e": {"value": fps_e2e, "unit": "frames/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "note": "vs_batch_step_host per step: pinned host frames in, pose heads out"},
+                    "note": "vs_batch_step_host per step: pinned host frames in (read over the host link by the step's "
+                             "first kernel), pose heads out"},
             "e2e_pageable": {"value": world * n_frames / e2e_pageable_s, "unit": "frames/s",
                              "note": "the same from pageable host frames"},
             "gpu_launches": int(kps * len(window)),
