@@ -30,7 +30,7 @@ def _same(a, b, tag):
     assert np.array_equal(a["w"], b["w"]), tag
     assert np.array_equal(a["tsdf"], b["tsdf"]), tag
     for l, (ma, mb) in enumerate(zip(a["maps"], b["maps"])):
-        for k in ("model_depth", "model_vertex", "model_normal", "model_img"):
+        for k in ("model_depth", "model_vertex", "model_normal", "model_img", "input_depth"):
             assert np.array_equal(ma[k], mb[k]), (tag, l, k)
 
 
@@ -40,14 +40,24 @@ def cases(gpu):
             helpers.make_case(width=320, height=240, dim=128, size=1.0, frames=FRAMES, seed=32)]
 
 
-def _run(cases, shape=None, tune_after=None):
+def _run(cases, shape=None, tune_after=None, device_frames=False):
     ss = [V.Session(c["cfg"]) for c in cases]
     snaps = []
     with V.Batch() as b:
         if shape is not None:
             b.set_launch_shape(*shape)
         for k in range(FRAMES):
-            b.step_host(ss, [c["depth"][k] for c in cases])
+            if device_frames:
+                # frames read in place by the step: the tuner's filter re-run
+                # reads the sessions' own copies, kept current by the ingest
+                torch = pytest.importorskip("torch")
+                fr = [torch.from_numpy(c["depth"][k].view(np.int16)).cuda() for c in cases]
+                torch.cuda.synchronize()
+                b.step(ss, [f.data_ptr() for f in fr])
+                b.sync()
+                del fr
+            else:
+                b.step_host(ss, [c["depth"][k] for c in cases])
             if tune_after == k:
                 before = [_snapshot(s) for s in ss]
                 best, ms = b.autotune(ss, reps=2)
@@ -70,9 +80,10 @@ def test_every_launch_shape_gives_the_same_results(cases):
             _same(a, b, "shape %s session %d" % (shape, i))
 
 
-def test_autotune_keeps_state_and_results(cases):
+@pytest.mark.parametrize("device_frames", [False, True])
+def test_autotune_keeps_state_and_results(cases, device_frames):
     ref = _run(cases)
-    got = _run(cases, tune_after=1)
+    got = _run(cases, tune_after=1, device_frames=device_frames)
     for i, (a, b) in enumerate(zip(ref, got)):
         _same(a, b, "tuned session %d" % i)
 

@@ -108,6 +108,11 @@ __global__ void __launch_bounds__(BX* R) k_bilateral_batch(const BatchTable* __r
     const uint16_t* __restrict__ mm = bt->frame[slot] ? bt->frame[slot] : s->depth_mm;
     bilateral_tile<true, R>(m, mm, nullptr, s->depth_scale, s->depth_raw, s->depth[0], W, H, (t % tw) * BX,
                             (t / tw) * R, g, s->lam_map ? s->dl_map : nullptr, s->lam_map);
+    if (mm != s->depth_mm) {
+      // a frame read in place: the session's own frame buffer is kept current
+      const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * R + threadIdx.y;
+      if (x < W && y < H) s->depth_mm[(size_t)y * W + x] = mm[(size_t)y * W + x];
+    }
     if (s->rgb_packed) {
       // the colour frame as one word per pixel, for the integration's gathers
       const int x = (t % tw) * BX + threadIdx.x, y = (t / tw) * R + threadIdx.y;

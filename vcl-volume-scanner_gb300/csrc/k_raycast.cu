@@ -82,9 +82,9 @@ struct Vol {
   // chained: the step after a box joins the run when it certainly reads 1
   // too, and the next box starts there.  The bounds are pulled in by 0.05
   // voxel, far more than the rounding of a position p + k inc (one product
-  // and one sum: under 1e-3 voxel for k <= kMaxRun and coordinates below
-  // 2048) or of the approximate reciprocals of the increment, so a step
-  // counted here reads 1 however its position rounds.  A negative result -k
+  // and one sum: under 1e-3 voxel wherever both p and the position lie within
+  // 2048 voxels of the volume) or of the approximate reciprocals of the
+  // increment, so a step counted here reads 1 however its position rounds.  A negative result -k
   // says p lies in a band brick that the ray leaves after about k steps; the
   // caller need not ask again before then (asking late only delays a run, it
   // never changes a sample).  A NaN coordinate fails every comparison below

@@ -126,8 +126,8 @@ struct BatchTable {
   int icp[kMaxLevels][kMaxSlots + 1];  // ICP block ranges per level
   int ray[kMaxSlots + 1];              // ray-cast tiles, all levels
   const uint16_t* frame[kMaxSlots];    // the uint16 frame each slot's ingest reads in place this step (device
-                                       // memory, or pinned host memory the device can address); NULL: the
-                                       // session's own frame buffer
+                                       // memory, or pinned host memory the device can address; the ingest
+                                       // also copies it into the session's frame buffer); NULL: that buffer
   int slab[kMaxSlots + 1];             // z slabs of bricks (band distance, x and y passes)
   int brow[kMaxSlots + 1];             // y rows of bricks (band distance, z pass)
   unsigned work[8];                    // work counters ([0..1] ray march, [2..3] ICP, [4..5] ray
