@@ -73,6 +73,10 @@ def test_null_arguments_rejected(built):
     assert lib.vs_scan_frame(None, None, None) == V.VS_ERR_ARG
     assert lib.vs_track_pose(None, None, None) == V.VS_ERR_ARG
     assert lib.vs_get_pose(None, None, None, None) == V.VS_ERR_ARG
+    assert lib.vs_get_band(None, None, None) == V.VS_ERR_ARG
+    assert lib.vs_get_icp_system(None, None, None) == V.VS_ERR_ARG
+    assert lib.vs_batch_step(None, None, 0, None, None) == V.VS_ERR_ARG
+    assert lib.vs_batch_step_host(None, None, 0, None, None, None) == V.VS_ERR_ARG
 
 
 def test_no_gpu_means_error_not_fallback(built):
