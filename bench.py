@@ -71,7 +71,7 @@ MIX = dict(name="serving_mix_64", sessions=64, seed=5, length=(50, 500),
            volumes=(128, 256, 384, 512), size_m=1.5, mu=0.02, mu_voxels=5.0, icp_iters=(10, 5, 4),
            th_icp=0.1 ** 2, normal_deg=20.0, dropout_blob=0.015, max_depth=2.5, arrival_fps=2000.0,
            hbm_budget_gb=150, p99_bound_ms=10.0,
-           serving_rates=(2000, 4000, 6000, 7000, 8000, 8500, 9000, 9500, 10000, 11000, 12000, 14000, 16000),
+           serving_rates=(2000, 4000, 6000, 7000, 8000, 8500, 9000, 9250, 9500, 10000, 11000, 12000, 14000, 16000),
            server_shapes=((3, 1), (1, 2)),
            plain_rates=(250, 500, 750, 1000, 1250, 1500, 1750, 2000, 2500))
 CPU_SESSIONS = 3  # the CPU sample: sessions 0..2, one of each frame size
