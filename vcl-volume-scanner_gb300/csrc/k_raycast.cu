@@ -495,7 +495,8 @@ __global__ void __launch_bounds__(kBandThreads) k_band_xy(const BatchTable* __re
       sx[i] = (uint8_t)band_window(sb, i, i - small_div(i, inv0) * nb0, nb0, 1);
     __syncthreads();
     uint8_t* __restrict__ out = s->btmp + (size_t)z * np;
-    for (int i = threadIdx.x; i < np; i += blockDim.x) out[i] = (uint8_t)band_window(sx, i, small_div(i, inv0), nb1, nb0);
+    for (int i = threadIdx.x; i < np; i += blockDim.x)
+      out[i] = (uint8_t)band_window(sx, i, small_div(i, inv0), nb1, nb0);
   }
 }
 
