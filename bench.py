@@ -476,6 +476,7 @@ def ate_all_sessions(specs, ours, ours_tracked, warm_depth, steps):
     dt = time.perf_counter() - t0
     per, worst, worst_i, worst_frame, all_rms = {}, 0.0, None, 0.0, 0.0
     lost_gpu, lost_oracle, sq, n_timed = {}, {}, 0.0, 0
+    sq_each, n_each = {}, {}
     for i, sp in enumerate(specs):
         rp, rt, _ = ref[i]
         d = np.linalg.norm(centres(ours[i]) - centres(rp), axis=1) * 1e3
@@ -483,6 +484,7 @@ def ate_all_sessions(specs, ours, ours_tracked, warm_depth, steps):
         if win.size:
             n_timed += win.size
             sq += float(np.sum(win ** 2))
+            sq_each[i], n_each[i] = float(np.sum(win ** 2)), win.size
             rms = float(np.sqrt(np.mean(win ** 2)))
             per["%d" % i] = round(rms, 5)
             if rms > worst:
@@ -495,7 +497,10 @@ def ate_all_sessions(specs, ours, ours_tracked, warm_depth, steps):
             lost_gpu["%d" % i] = g_lost[:20]
         if o_lost:
             lost_oracle["%d" % i] = o_lost[:20]
+    rest = [i for i in sq_each if i != worst_i]
     out = {"vs_fp64_oracle_mm": worst, "pooled_rms_mm": float(np.sqrt(sq / max(1, n_timed))),
+           "pooled_rms_mm_without_worst_session": float(np.sqrt(sum(sq_each[i] for i in rest) /
+                                                                max(1, sum(n_each[i] for i in rest)))),
            "sessions_within_1mm": int(sum(1 for v in per.values() if v < 1.0)), "worst_frame_mm": worst_frame,
            "all_frames_worst_session_mm": all_rms, "sessions": len(per), "timed_frames_compared": int(n_timed),
            "per_session_rms_mm": per, "sessions_with_lost_frames": {"gpu": lost_gpu, "fp64_oracle": lost_oracle},
